@@ -1,0 +1,198 @@
+/*
+ * wstack_gb300.h -- C ABI of the GB300 (sm_103a) w-stacking library
+ * (lofar_gb300/libwstack_gb300.so).
+ *
+ * Two layers:
+ *
+ * 1. Drop-in symbols with the reference's exact signatures and argument
+ *    meaning (nandhanas/LOFAR, w-stacking.h).  A reference build links this
+ *    library instead of compiling w-stacking.cu / phase_correction.cu.  All
+ *    pointers may be ordinary host memory (the reference's contract) or device
+ *    memory; the library detects which.  They return void like the reference;
+ *    failures are recorded for wstack_gb300_last_error().
+ *
+ * 2. A device-resident plan API (wsg_*).  The grid stays in HBM between
+ *    gridding, the per-plane FFT and the w-correction (the reference's
+ *    MPI/NUMA reduction collapses to this resident grid).  All data pointers
+ *    are device pointers unless the name ends in _host.  Every call returns a
+ *    wsg_status.  Calls are ordered on the plan's CUDA stream.
+ *
+ * Layouts (as in the reference):
+ *   uu, vv, ww    double[num_points], normalised so that cell = (int)(uu/dx),
+ *                 plane = (int)(ww/dw)            (w-stacking.cu:66-71)
+ *   vis_real/img  float[num_points*freq_per_chan*polarizations], [m][f][p]
+ *   weight        float[num_points*polarizations], [m][p]
+ *   grid          [plane][v][u] complex (re, im interleaved); complex128 for
+ *                 WSG_FP64, complex64 for WSG_FP32C    (w-stacking.cu:90)
+ *   image         [v][u] complex, same precision as the plan's grid
+ */
+#ifndef WSTACK_GB300_H_
+#define WSTACK_GB300_H_
+
+#if defined(__GNUC__)
+#define WSG_API __attribute__((visibility("default")))
+#else
+#define WSG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* 1. Drop-in entry points (reference signatures)                      */
+/* ------------------------------------------------------------------ */
+
+/*
+ * Replaces wstack() (declared w-stacking.h:12-29; CUDA body
+ * w-stacking.cu:123-220; OpenMP body w-stacking.cu:222-311).
+ * Grids num_points measurements into grid[num_w_planes][grid_size_y]
+ * [grid_size_x][2] (FP64).  Like the reference's CUDA build the grid is
+ * overwritten (the OpenMP build accumulates; the two agree on a zeroed grid,
+ * which is what the reference's caller passes, init.c:369).  num_threads is
+ * accepted and ignored.  Measurements whose w-plane index is outside
+ * [0, num_w_planes) are skipped and counted (the reference writes outside the
+ * grid for them).  The precision is FP64 unless wstack_gb300_set_precision()
+ * selected WSG_FP32C.
+ */
+WSG_API void wstack(int num_w_planes, long num_points, long freq_per_chan, long polarizations,
+            double *uu, double *vv, double *ww, float *vis_real, float *vis_img,
+            float *weight, double dx, double dw, int w_support, int grid_size_x,
+            int grid_size_y, double *grid, int num_threads);
+
+/*
+ * Replaces phase_correction() (declared w-stacking.h:39-51; definition
+ * phase_correction.cu:89-212, PHASE_ON).  gridss is the per-plane FFT output
+ * already scaled by 1/(Nx*Ny) (fourier_transform.c:56-57); image_real and
+ * image_imag ([yaxis][xaxis] doubles) are overwritten, like the reference's
+ * CUDA build.  Pixels with sin^2+sin^2 > 1 come out NaN exactly as in the
+ * reference.  num_threads is ignored.
+ */
+WSG_API void phase_correction(double *gridss, double *image_real, double *image_imag, int xaxis,
+                      int yaxis, int num_w_planes, int xaxistot, int yaxistot,
+                      double resolution, double wmin, double wmax, int num_threads);
+
+/* Replaces test() (w-stacking.h:34, w-stacking.cu:316-322): returns nnn+1. */
+WSG_API int test(int nnn);
+
+/*
+ * The per-plane inverse FFT of fftw_data() (fourier_transform.c:25-59), which
+ * the reference runs inline with FFTW over globals: for each of nplanes
+ * planes, out = (1/(nx*ny)) * sum_k in_k e^{+2 pi i k.x/n} (FFTW_BACKWARD).
+ * in and out are [nplanes][ny][nx] complex128 and may alias.  Returns a
+ * wsg_status.  A patched fftw_data() calls this instead of fftw_execute().
+ */
+WSG_API int wstack_fft_planes(const double *in, double *out, int nx, int ny, int nplanes);
+
+/* Status of the last drop-in call made by this thread (wsg_status). */
+WSG_API int wstack_gb300_last_error(void);
+/* Human-readable message for the last drop-in failure of this thread. */
+WSG_API const char *wstack_gb300_last_error_string(void);
+/* Precision used by the drop-in wstack()/phase_correction(): WSG_FP64
+ * (default) or WSG_FP32C.  Returns the previous value, or -1 if invalid. */
+WSG_API int wstack_gb300_set_precision(int precision);
+/* Frees the device state that the drop-in calls keep between calls. */
+WSG_API void wstack_gb300_release(void);
+
+/* ------------------------------------------------------------------ */
+/* 2. Device-resident plan API                                         */
+/* ------------------------------------------------------------------ */
+
+typedef enum {
+    WSG_OK = 0,
+    WSG_ERR_ARG = 1,        /* invalid argument (size, pointer, support)   */
+    WSG_ERR_CUDA = 2,       /* a CUDA runtime call failed                  */
+    WSG_ERR_CUFFT = 3,      /* a cuFFT call failed                         */
+    WSG_ERR_NOMEM = 4,      /* device allocation failed                    */
+    WSG_ERR_STATE = 5,      /* call out of order (e.g. adjoint before bin) */
+    WSG_ERR_CAPACITY = 6,   /* more points than the reserved capacity      */
+    WSG_ERR_UNSUPPORTED = 7 /* configuration outside the kernels' limits   */
+} wsg_status;
+
+typedef enum {
+    WSG_FP64 = 0,   /* FP64 grid, FFT and w-correction: the reference's arithmetic */
+    WSG_FP32C = 1   /* complex64 grid with compensated (two-float) tile
+                       accumulation; FP64-exact coordinates and phase argument */
+} wsg_precision;
+
+typedef struct wsg_plan wsg_plan;
+
+typedef struct {
+    long long points_in;        /* measurements passed to the last wsg_bin   */
+    long long records;          /* (measurement, tile) records written       */
+    long long dropped_plane;    /* skipped: w-plane index outside [0, P)      */
+    long long dropped_window;   /* skipped: support window entirely off-grid  */
+    int bins;                   /* number of (plane, tile) bins              */
+    int tile;                   /* tile edge in cells                        */
+    int max_bin_records;        /* largest bin                               */
+    int ctas;                   /* persistent CTAs launched per kernel       */
+} wsg_stats;
+
+/*
+ * Creates a plan for a [num_w_planes][grid_size_y][grid_size_x] grid.
+ * dx, dw: as passed to wstack() (dx = 1/Nx, dw = 1/P in the reference,
+ * init.c:16-17).  w_support: kernel support in cells (odd, 1..15).
+ * stream: a cudaStream_t (NULL = the legacy default stream).
+ */
+WSG_API int wsg_plan_create(wsg_plan **plan, int grid_size_x, int grid_size_y, int num_w_planes,
+                    int w_support, double dx, double dw, int precision, void *stream);
+WSG_API int wsg_plan_destroy(wsg_plan *plan);
+WSG_API int wsg_plan_set_stream(wsg_plan *plan, void *stream);
+/* Tile edge (32 or 64 cells) and persistent CTA count (0 = automatic). */
+WSG_API int wsg_plan_set_tuning(wsg_plan *plan, int tile, int ctas, int chunk);
+/* Reserves device memory for up to max_points measurements so that later
+ * calls allocate nothing (required before CUDA-graph capture). */
+WSG_API int wsg_plan_reserve(wsg_plan *plan, long max_points);
+/* W-correction geometry (phase_correction's resolution, wmin, wmax). */
+WSG_API int wsg_plan_set_wcorrection(wsg_plan *plan, double resolution, double wmin, double wmax);
+WSG_API int wsg_plan_get_stats(wsg_plan *plan, wsg_stats *stats);
+/* Bytes of device memory the plan holds. */
+WSG_API long long wsg_plan_device_bytes(wsg_plan *plan);
+
+/* Sort measurements into (w-plane, tile) bins and fold vis*weight over
+ * frequency and polarisation (w-stacking.cu:98-112).  Device pointers. */
+WSG_API int wsg_bin(wsg_plan *plan, long num_points, long freq_per_chan, long polarizations,
+            const double *uu, const double *vv, const double *ww, const float *vis_real,
+            const float *vis_img, const float *weight);
+/* Grid the binned measurements; grid is overwritten (every cell written). */
+WSG_API int wsg_grid(wsg_plan *plan, void *grid);
+/* Unnormalised per-plane 2D FFT in place; sign +1 = exponent +i
+ * (FFTW_BACKWARD, the forward imaging direction), -1 = exponent -i. */
+WSG_API int wsg_fft(wsg_plan *plan, void *grid, int sign);
+/* image = sum_w planes_w * e^{i phi_w} * dwnorm * sqrt(1-r^2) * scale
+ * (phase_correction.cu:36-80); scale = 1/(Nx*Ny) folds in the FFT norm. */
+WSG_API int wsg_wcorrect(wsg_plan *plan, const void *planes, void *image, double scale);
+/* Adjoint of wsg_wcorrect: planes_w = conj(e^{i phi_w}) * dwnorm *
+ * sqrt(1-r^2) * scale * image. */
+WSG_API int wsg_wcorrect_adjoint(wsg_plan *plan, const void *image, void *planes, double scale);
+/* Adjoint of wsg_grid for the measurements of the last wsg_bin:
+ * out[m] = sum over m's support window of kernel weight * grid (complex,
+ * plan precision), [num_points] complex, overwritten. */
+WSG_API int wsg_degrid(wsg_plan *plan, const void *grid, void *out);
+
+/* Forward imaging: bin + grid + FFT + w-correction into image
+ * ([Ny][Nx] complex, plan precision).  Uses the plan's resident grid. */
+WSG_API int wsg_image_forward(wsg_plan *plan, long num_points, long freq_per_chan, long polarizations,
+                      const double *uu, const double *vv, const double *ww,
+                      const float *vis_real, const float *vis_img, const float *weight,
+                      void *image);
+/* Adjoint imaging for the measurements of the last wsg_image_forward/wsg_bin:
+ * out[m] (complex, plan precision) = (A^H image)[m]. */
+WSG_API int wsg_image_adjoint(wsg_plan *plan, const void *image, void *out);
+
+/* Same as wsg_image_forward / wsg_image_adjoint with HOST buffers; the copies
+ * to and from the device are part of the call, which returns when the host
+ * outputs are written. */
+WSG_API int wsg_image_forward_host(wsg_plan *plan, long num_points, long freq_per_chan,
+                           long polarizations, const double *uu, const double *vv,
+                           const double *ww, const float *vis_real, const float *vis_img,
+                           const float *weight, void *image);
+WSG_API int wsg_image_adjoint_host(wsg_plan *plan, const void *image, void *out);
+
+/* Resident grid of the plan ([P][Ny][Nx] complex), for inspection. */
+WSG_API void *wsg_plan_grid(wsg_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WSTACK_GB300_H_ */

@@ -1,0 +1,114 @@
+"""ctypes binding of libwstack_gb300.so (the C ABI in include/wstack_gb300.h).
+
+The library is required: there is no CPU or pure-PyTorch fallback.  If it is
+missing, loading raises immediately with the command that builds it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libwstack_gb300.so")
+
+WSG_OK = 0
+WSG_ERR_ARG = 1
+WSG_ERR_CUDA = 2
+WSG_ERR_CUFFT = 3
+WSG_ERR_NOMEM = 4
+WSG_ERR_STATE = 5
+WSG_ERR_CAPACITY = 6
+WSG_ERR_UNSUPPORTED = 7
+
+WSG_FP64 = 0
+WSG_FP32C = 1
+
+STATUS_NAMES = {0: "WSG_OK", 1: "WSG_ERR_ARG", 2: "WSG_ERR_CUDA", 3: "WSG_ERR_CUFFT",
+                4: "WSG_ERR_NOMEM", 5: "WSG_ERR_STATE", 6: "WSG_ERR_CAPACITY",
+                7: "WSG_ERR_UNSUPPORTED"}
+
+
+class WstackError(RuntimeError):
+    """A call into libwstack_gb300.so returned a non-zero wsg_status."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("points_in", ctypes.c_longlong), ("records", ctypes.c_longlong),
+                ("dropped_plane", ctypes.c_longlong), ("dropped_window", ctypes.c_longlong),
+                ("bins", ctypes.c_int), ("tile", ctypes.c_int), ("max_bin_records", ctypes.c_int),
+                ("ctas", ctypes.c_int)]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+_L = ctypes.c_long
+
+# name -> (restype, argtypes); every symbol of include/wstack_gb300.h
+SIGNATURES = {
+    "wstack": (None, [_I, _L, _L, _L, _P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P, _I]),
+    "phase_correction": (None, [_P, _P, _P, _I, _I, _I, _I, _I, _D, _D, _D, _I]),
+    "test": (_I, [_I]),
+    "wstack_fft_planes": (_I, [_P, _P, _I, _I, _I]),
+    "wstack_gb300_last_error": (_I, []),
+    "wstack_gb300_last_error_string": (ctypes.c_char_p, []),
+    "wstack_gb300_set_precision": (_I, [_I]),
+    "wstack_gb300_release": (None, []),
+    "wsg_plan_create": (_I, [ctypes.POINTER(_P), _I, _I, _I, _I, _D, _D, _I, _P]),
+    "wsg_plan_destroy": (_I, [_P]),
+    "wsg_plan_set_stream": (_I, [_P, _P]),
+    "wsg_plan_set_tuning": (_I, [_P, _I, _I, _I]),
+    "wsg_plan_reserve": (_I, [_P, _L]),
+    "wsg_plan_set_wcorrection": (_I, [_P, _D, _D, _D]),
+    "wsg_plan_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
+    "wsg_plan_device_bytes": (ctypes.c_longlong, [_P]),
+    "wsg_plan_grid": (_P, [_P]),
+    "wsg_bin": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P]),
+    "wsg_grid": (_I, [_P, _P]),
+    "wsg_fft": (_I, [_P, _P, _I]),
+    "wsg_wcorrect": (_I, [_P, _P, _P, _D]),
+    "wsg_wcorrect_adjoint": (_I, [_P, _P, _P, _D]),
+    "wsg_degrid": (_I, [_P, _P, _P]),
+    "wsg_image_forward": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
+    "wsg_image_adjoint": (_I, [_P, _P, _P]),
+    "wsg_image_forward_host": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
+    "wsg_image_adjoint_host": (_I, [_P, _P, _P]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load libwstack_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "or `python lofar_gb300/build.py` (requires nvcc)")
+    lib = ctypes.CDLL(p, mode=ctypes.RTLD_GLOBAL)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != WSG_OK:
+        msg = load().wstack_gb300_last_error_string()
+        raise WstackError(status, msg.decode() if msg else "")
+
+
+def last_error() -> tuple[int, str]:
+    lib = load()
+    msg = lib.wstack_gb300_last_error_string()
+    return lib.wstack_gb300_last_error(), (msg.decode() if msg else "")

@@ -1,0 +1,123 @@
+// Internal declarations shared by the translation units of libwstack_gb300.so.
+//
+// Data layout in HBM (one plan, P planes of Ny x Nx cells, tile edge T):
+//   grid      [P][Ny][Nx] complex (float2 for FP32C, double2 for FP64),
+//             the reference's [w][v][u][re,im] layout (w-stacking.cu:90)
+//   bins      (plane, tile-row, tile-col) in row-major order,
+//             bin = (w*ntv + tv)*ntu + tu; per-bin record counts, offsets
+//   records   structure-of-arrays, grouped by bin, primaries first:
+//             rec_cell  u32   (cu + 32768) | (cv + 32768) << 16, the
+//                             measurement's cell relative to the tile origin
+//             rec_frac  float2/double2   pos - cell (exact in FP64)
+//             rec_val   float2/double2   sum_{f,p} weight*vis (the fold of
+//                             w-stacking.cu:98-112)
+//             rec_idx   u32   original measurement index
+//   A measurement whose support window touches k tiles has k records
+//   (halo duplication, k <= 4); the record in the tile holding its own
+//   (clamped) cell is its primary.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include "wstack_gb300.h"
+
+namespace wsg {
+
+// The reference's pi (w-stacking.h:6), kept for bit-level parity.
+constexpr double kRefPi = 3.14159265359;
+
+constexpr int kMaxHalf = 7;          // support up to 15 cells
+constexpr int kThreads = 256;        // threads per CTA for tile kernels
+
+struct DevCounters {
+    unsigned long long records;
+    unsigned long long dropped_plane;
+    unsigned long long dropped_window;
+    unsigned int max_bin;
+    unsigned int work_grid;
+    unsigned int work_degrid;
+    unsigned int error;
+    unsigned int pad[2];
+};
+
+// Geometry of the coordinate step (w-stacking.cu:66-77) and the tiling.
+struct GeomParams {
+    int nx, ny, planes, half, tile, ntu, ntv;
+    int u_pow2, w_pow2;   // dx (dw) is an exact power of two: 1/dx == 2^ku
+    int ku, kw;
+    double dx, dw;
+    long long nbins;
+};
+
+struct BinBuffers {
+    unsigned *cnt_prim, *cnt_dup, *cur_prim, *cur_dup, *off, *order;
+    DevCounters *ctr;
+};
+
+struct RecBuffers {
+    unsigned *cell;
+    void *frac;   // float2 or double2
+    void *val;    // float2 or double2
+    unsigned *idx;
+    unsigned long long capacity;
+};
+
+// Pixel-geometry table of the FP32C w-correction (per pixel, planar):
+// the phase in cycles for plane w is a + w*b (mod 1), a and b as
+// float-float pairs reduced to [-0.5, 0.5]; amp = dwnorm*sqrt(1-r^2).
+struct WScreen {
+    float *ah, *al, *bh, *bl, *amp;
+    double *sinx, *siny;
+};
+
+// ---- launchers (bin.cu) ----
+cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double *vv,
+                             const double *ww, long long n, const BinBuffers &b,
+                             cudaStream_t s);
+cudaError_t launch_bin_scan(const GeomParams &g, const BinBuffers &b, cudaStream_t s);
+cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu,
+                               const double *vv, const double *ww, const float *vr,
+                               const float *vi, const float *wt, long long n, long long nf,
+                               long long np, const BinBuffers &b, const RecBuffers &r,
+                               cudaStream_t s);
+
+// ---- launchers (grid.cu) ----
+cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b,
+                        const RecBuffers &r, void *grid, int ctas, int chunk,
+                        cudaStream_t s);
+int grid_max_ctas_per_sm(int prec, int tile, int half);
+
+// ---- launchers (degrid.cu) ----
+cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b,
+                          const RecBuffers &r, const void *grid, void *out, long long n,
+                          int ctas, cudaStream_t s);
+int degrid_max_ctas_per_sm(int prec, int tile, int half);
+
+// ---- launchers (wcorrect.cu) ----
+struct WcParams {
+    int xaxis, yaxis, planes, xaxistot, yaxistot;
+    double resolution, wmin, wmax;
+    int phase_on;
+};
+cudaError_t launch_wscreen_tables(const WcParams &p, double *sinx, double *siny,
+                                  cudaStream_t s);
+cudaError_t launch_wscreen_build(const WcParams &p, const WScreen &ws, cudaStream_t s);
+cudaError_t launch_wcorrect_f32c(const WcParams &p, const WScreen &ws, const float2 *planes,
+                                 float2 *image, double scale, cudaStream_t s);
+cudaError_t launch_wcorrect_adj_f32c(const WcParams &p, const WScreen &ws, const float2 *image,
+                                     float2 *planes, double scale, cudaStream_t s);
+cudaError_t launch_wcorrect_f64(const WcParams &p, const double *sinx, const double *siny,
+                                const double2 *planes, double2 *image, double *image_re,
+                                double *image_im, double scale, cudaStream_t s);
+cudaError_t launch_wcorrect_adj_f64(const WcParams &p, const double *sinx, const double *siny,
+                                    const double2 *image, double2 *planes, double scale,
+                                    cudaStream_t s);
+cudaError_t launch_scale_f64(double2 *x, long long n, double scale, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double2 *in, float2 *out, long long n, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const float2 *in, double2 *out, long long n, cudaStream_t s);
+
+int num_sms();
+
+}  // namespace wsg

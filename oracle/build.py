@@ -1,0 +1,80 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+Two shared libraries are produced:
+
+* ``oracle/_build/liboracle.so`` -- the C restatement in ``wstack_oracle.c``.
+  It is compiled wherever the tests run (here and on the GPU host).
+* ``oracle/_ref/libref.so`` -- the reference's own CPU path, compiled straight
+  from the reference tree (``w-stacking.cu`` and ``phase_correction.cu`` as C,
+  ``-DPHASE_ON``, exactly as the reference's Makefile copies them to ``.c``).
+  It is built only when the reference tree is present; its sources are never
+  copied into this repository.
+
+Both use the same flags (``-O2 -ffp-contract=off``) so that a single-threaded
+run of one is bit-identical to the other on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
+REF_SO = os.path.join(REF_DIR, "libref.so")
+REFERENCE_TREE = os.environ.get("WSTACK_REFERENCE_TREE", "/root/reference")
+
+CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"]
+
+
+def _newer(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "wstack_oracle.c")
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not _newer(ORACLE_SO, [src, __file__]):
+        cmd = ["gcc", *CFLAGS, src, "-o", ORACLE_SO, "-lm"]
+        subprocess.run(cmd, check=True)
+    return ORACLE_SO
+
+
+def reference_sources() -> list[str] | None:
+    srcs = [os.path.join(REFERENCE_TREE, f) for f in ("w-stacking.cu", "phase_correction.cu")]
+    if all(os.path.exists(s) for s in srcs):
+        return srcs
+    return None
+
+
+def build_ref(force: bool = False) -> str | None:
+    """Compile the reference's CPU gridding + phase correction, if present."""
+    srcs = reference_sources()
+    if srcs is None:
+        return REF_SO if os.path.exists(REF_SO) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    if force or not _newer(REF_SO, srcs + [__file__]):
+        # -x c: the reference's Makefile copies these .cu files to .c and
+        # compiles them with the C compiler (Makefile:51-55); the __CUDACC__
+        # branches are then excluded and the OpenMP CPU bodies are used.
+        cmd = ["gcc", "-x", "c", *CFLAGS, "-DPHASE_ON", f"-I{REFERENCE_TREE}", *srcs,
+               "-x", "none", "-o", REF_SO, "-lm"]
+        subprocess.run(cmd, check=True)
+    return REF_SO
+
+
+def main() -> int:
+    force = "--force" in sys.argv
+    print(build_oracle(force))
+    print(build_ref(force))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
