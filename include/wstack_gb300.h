@@ -192,6 +192,31 @@ WSG_API int wsg_image_adjoint_host(wsg_plan *plan, const void *image, void *out)
 /* Resident grid of the plan ([P][Ny][Nx] complex), for inspection. */
 WSG_API void *wsg_plan_grid(wsg_plan *plan);
 
+/*
+ * FP64 gridding that allocates no device memory.  It has no counterpart in
+ * the reference; it is for callers that cannot call cudaMalloc when they grid
+ * (a real-time pipeline that reserves all device memory up front, a host
+ * application that owns the device memory and lends a plug-in only its own
+ * buffers, code that must not synchronise the device with an allocation).
+ * Arguments and results are those of wstack() (FP64, grid overwritten), but
+ * every pointer must be device memory and the call is asynchronous on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).
+ * Its scratch is a fixed 64 MiB static device array per GPU, held until the
+ * process exits; a call needing more than
+ *     256 + 24*nbins + 160*num_points bytes (+ alignment),
+ *     nbins = num_w_planes*ceil(grid_size_y/64)*ceil(grid_size_x/64),
+ * fails with WSG_ERR_CAPACITY (about 400,000 measurements on a 4096x4096x32
+ * grid).  All calls share that array: calls whose GPU work may overlap race
+ * and must be serialised by the caller.  The first call on a device looks up
+ * the array's device address and may load the device code: make it before
+ * any stream capture.
+ */
+WSG_API int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per_chan,
+                             long polarizations, const double *uu, const double *vv,
+                             const double *ww, const float *vis_real, const float *vis_img,
+                             const float *weight, double dx, double dw, int w_support,
+                             int grid_size_x, int grid_size_y, double *grid, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,7 @@ SIGNATURES = {
     "wsg_image_adjoint": (_I, [_P, _P, _P]),
     "wsg_image_forward_host": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
     "wsg_image_adjoint_host": (_I, [_P, _P, _P]),
+    "wsg_grid_noalloc": (_I, [_I, _L, _L, _L, _P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P, _P]),
 }
 
 _lib = None

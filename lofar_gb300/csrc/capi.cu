@@ -112,6 +112,13 @@ bool device_accessible(const void *ptr)
 
 }  // namespace
 
+// Records a status and message as this thread's last error (for entry points
+// defined in other translation units).
+int wsg::report_status(int status, const char *msg)
+{
+    return set_error(status, "%s", msg ? msg : "");
+}
+
 int wsg::num_sms()
 {
     static int n = 0;

@@ -119,5 +119,6 @@ cudaError_t launch_f64_to_f32(const double2 *in, float2 *out, long long n, cudaS
 cudaError_t launch_f32_to_f64(const float2 *in, double2 *out, long long n, cudaStream_t s);
 
 int num_sms();
+int report_status(int status, const char *msg);
 
 }  // namespace wsg
