@@ -157,7 +157,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 STAGES = ["bin", "grid", "fft_fwd", "wcorrect", "wcorrect_adj", "fft_adj", "degrid"]
-OUR_KERNELS_PER_STEP = {"bin": 3, "grid": 1, "fft_fwd": 0, "wcorrect": 1, "wcorrect_adj": 1,
+OUR_KERNELS_PER_STEP = {"bin": 5, "grid": 1, "fft_fwd": 0, "wcorrect": 1, "wcorrect_adj": 1,
                         "fft_adj": 0, "degrid": 1}
 
 

@@ -138,7 +138,9 @@ WSG_API int wsg_plan_create(wsg_plan **plan, int grid_size_x, int grid_size_y, i
                     int w_support, double dx, double dw, int precision, void *stream);
 WSG_API int wsg_plan_destroy(wsg_plan *plan);
 WSG_API int wsg_plan_set_stream(wsg_plan *plan, void *stream);
-/* Tile edge (32 or 64 cells) and persistent CTA count (0 = automatic). */
+/* Tile edge (32 or 64 cells), persistent CTA count and split size (records
+ * per work item of a bin cut into several; >= 512) -- 0 keeps the current
+ * value (ctas 0 = automatic). */
 WSG_API int wsg_plan_set_tuning(wsg_plan *plan, int tile, int ctas, int chunk);
 /* Reserves device memory for up to max_points measurements so that later
  * calls allocate nothing (required before CUDA-graph capture). */
@@ -203,7 +205,8 @@ WSG_API void *wsg_plan_grid(wsg_plan *plan);
  * `stream` (a cudaStream_t, NULL = legacy default stream).
  * Its scratch is a fixed 64 MiB static device array per GPU, held until the
  * process exits; a call needing more than
- *     256 + 24*nbins + 160*num_points bytes (+ alignment),
+ *     256 + 24*nbins + 8*ceil(nbins/4096) + 32768 + 160*num_points bytes
+ *     (+ alignment),
  *     nbins = num_w_planes*ceil(grid_size_y/64)*ceil(grid_size_x/64),
  * fails with WSG_ERR_CAPACITY (about 400,000 measurements on a 4096x4096x32
  * grid).  All calls share that array: calls whose GPU work may overlap race

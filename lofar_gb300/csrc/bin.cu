@@ -3,11 +3,18 @@
 // Replaces the reference's per-rank v-slab decomposition (gridding.c:35-86)
 // with a device-side sort whose key reuses the reference's own coordinate
 // step (w-stacking.cu:66-77), so every measurement lands on exactly the cells
-// and plane the reference would use.  Three kernels, all HBM-streaming:
-//   k_bin_count   one pass over uvw: per-bin record counts (primary/duplicate)
-//   k_bin_scan    exclusive scan of the counts + a longest-first bin order
-//   k_bin_scatter second pass over all inputs: writes the SoA records
+// and plane the reference would use.  Five short kernels:
+//   k_bin_count    one pass over uvw: per-bin record counts (primary/duplicate)
+//   k_bin_scan_a   per-CTA sums of bin sizes and of split work items
+//   k_bin_scan_b   one CTA: scan of the per-CTA sums
+//   k_bin_scan_c   per-bin record offsets; bins above the split size are cut
+//                  into work items of at most that many records
+//   k_bin_scatter  second pass over all inputs: writes the records
+// The tile kernels take the split items first, then every other bin, so no
+// work item holds more than `split` records and the load stays balanced.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "coord.cuh"
 #include "wsg_internal.cuh"
@@ -59,203 +66,349 @@ __device__ __forceinline__ unsigned bin_index(const GeomParams &g, int w, int tv
     return (unsigned)(((long long)w * g.ntv + tv) * g.ntu + tu);
 }
 
+// Both passes give each thread kItems measurements per sweep (item i of a
+// thread at base + i*blockDim + tid, so each item slot is a coalesced load);
+// their loads and atomics are independent, which keeps several memory
+// operations in flight per thread.
+constexpr int kItems = 4;
+
 template <bool UP2, bool WP2>
 __global__ void __launch_bounds__(256)
 k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
             const double *__restrict__ ww, long long n, BinBuffers b)
 {
     const int lane = threadIdx.x & 31;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const long long m = base + threadIdx.x;
-        int st = 3;
-        MGeom o;
-        if (m < n) {
+    const long long stride = (long long)gridDim.x * blockDim.x * kItems;
+    for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
+        double x[kItems], y[kItems], z[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+            x[i] = m < n ? __ldcs(uu + m) : 0.0;
+            y[i] = m < n ? __ldcs(vv + m) : 0.0;
+            z[i] = m < n ? __ldcs(ww + m) : 0.0;
+        }
+        int ndp = 0, ndw = 0;
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+            MGeom o;
             float fu, fv;
-            st = measure<UP2, WP2, float>(g, __ldg(uu + m), __ldg(vv + m), __ldg(ww + m), o, fu,
-                                          fv);
+            const int st = m < n ? measure<UP2, WP2, float>(g, x[i], y[i], z[i], o, fu, fv) : 3;
+            ndp += st == 1;
+            ndw += st == 2;
+            const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
+            const unsigned peers = __match_any_sync(kFull, prim);
+            if (st == 0) {
+                if (lane == __ffs(peers) - 1) atomicAdd(&b.cnt_prim[prim], (unsigned)__popc(peers));
+                for (int tv = o.tv0; tv <= o.tv1; tv++)
+                    for (int tu = o.tu0; tu <= o.tu1; tu++)
+                        if (tv != o.tvp || tu != o.tup)
+                            atomicAdd(&b.cnt_dup[bin_index(g, o.gw, tv, tu)], 1u);
+            }
         }
-        const unsigned dp = __ballot_sync(kFull, st == 1);
-        const unsigned dwn = __ballot_sync(kFull, st == 2);
+        for (int d = 16; d >= 1; d >>= 1) {
+            ndp += __shfl_xor_sync(kFull, ndp, d);
+            ndw += __shfl_xor_sync(kFull, ndw, d);
+        }
         if (lane == 0) {
-            if (dp) atomicAdd(&b.ctr->dropped_plane, (unsigned long long)__popc(dp));
-            if (dwn) atomicAdd(&b.ctr->dropped_window, (unsigned long long)__popc(dwn));
-        }
-        const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
-        const unsigned peers = __match_any_sync(kFull, prim);
-        if (st == 0) {
-            if (lane == __ffs(peers) - 1) atomicAdd(&b.cnt_prim[prim], (unsigned)__popc(peers));
-            for (int tv = o.tv0; tv <= o.tv1; tv++)
-                for (int tu = o.tu0; tu <= o.tu1; tu++)
-                    if (tv != o.tvp || tu != o.tup)
-                        atomicAdd(&b.cnt_dup[bin_index(g, o.gw, tv, tu)], 1u);
+            if (ndp) atomicAdd(&b.ctr->dropped_plane, (unsigned long long)ndp);
+            if (ndw) atomicAdd(&b.ctr->dropped_window, (unsigned long long)ndw);
         }
     }
 }
 
-template <typename F2> struct Vec2;
-template <> struct Vec2<float2> {
-    using S = float;
-    static __device__ __forceinline__ float2 make(float a, float b) { return make_float2(a, b); }
-};
-template <> struct Vec2<double2> {
-    using S = double;
-    static __device__ __forceinline__ double2 make(double a, double b)
-    {
-        return make_double2(a, b);
-    }
-};
-
-// The fold of w-stacking.cu:98-112 taken out of the tap loop: the product
-// weight*vis is formed in float (float*float), entries whose real part is
-// NaN are skipped; the FP64 form sums the promoted products in double.
 template <typename S>
 __device__ __forceinline__ void fold_value(const float *__restrict__ vr,
                                            const float *__restrict__ vi,
                                            const float *__restrict__ wt, long long m,
                                            long long nf, long long np, S &re, S &im)
 {
+    // the fold of w-stacking.cu:98-112 taken out of the tap loop: weight*vis
+    // is a float product; entries whose real part is NaN are skipped
     re = 0;
     im = 0;
     const long long vb = m * nf * np;
     const long long wb = m * np;
     for (long long f = 0; f < nf; f++) {
         for (long long p = 0; p < np; p++) {
-            const float a = __ldg(vr + vb + f * np + p);
+            const float a = __ldcs(vr + vb + f * np + p);
             if (!isnan(a)) {
-                const float w = __ldg(wt + wb + p);
-                const float b = __ldg(vi + vb + f * np + p);
+                const float w = __ldcs(wt + wb + p);
+                const float c = __ldcs(vi + vb + f * np + p);
                 re += (S)(w * a);
-                im += (S)(w * b);
+                im += (S)(w * c);
             }
         }
     }
 }
 
-template <bool UP2, bool WP2, typename F2>
+// The FP32C record (16 bytes): per axis one word, the tile-relative cell in
+// the top 8 bits (biased by 64) and (frac + 1) * 2^23 in the low 24 bits,
+// then the folded value as two floats.
+__device__ __forceinline__ unsigned pack_axis(int c, float f)
+{
+    unsigned q = (unsigned)__float2int_rn((f + 1.0f) * 8388608.0f);
+    q = min(q, 0xFFFFFFu);
+    return ((unsigned)(c + 64) << 24) | q;
+}
+
+template <bool UP2, bool WP2, int PREC>
 __global__ void __launch_bounds__(256)
 k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
               const double *__restrict__ ww, const float *__restrict__ vr,
               const float *__restrict__ vi, const float *__restrict__ wt, long long n,
               long long nf, long long np, BinBuffers b, RecBuffers r)
 {
-    using S = typename Vec2<F2>::S;
-    F2 *frac = reinterpret_cast<F2 *>(r.frac);
-    F2 *val = reinterpret_cast<F2 *>(r.val);
+    using S = typename std::conditional<PREC == WSG_FP64, double, float>::type;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const long long m = base + threadIdx.x;
-        int st = 3;
-        MGeom o;
-        S fu = 0, fv = 0;
-        if (m < n) st = measure<UP2, WP2, S>(g, __ldg(uu + m), __ldg(vv + m), __ldg(ww + m), o, fu, fv);
-        const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
-        const unsigned peers = __match_any_sync(kFull, prim);
-        const int leader = __ffs(peers) - 1;
-        unsigned got = 0;
-        if (st == 0 && lane == leader) got = atomicAdd(&b.cur_prim[prim], (unsigned)__popc(peers));
-        const unsigned basep = __shfl_sync(kFull, got, leader);
-        if (st != 0) continue;
-
-        S re, im;
-        fold_value<S>(vr, vi, wt, m, nf, np, re, im);
-        const F2 fr = Vec2<F2>::make(fu, fv);
-        const F2 vv2 = Vec2<F2>::make(re, im);
-        for (int tv = o.tv0; tv <= o.tv1; tv++) {
-            for (int tu = o.tu0; tu <= o.tu1; tu++) {
-                const unsigned bin = bin_index(g, o.gw, tv, tu);
-                unsigned pos;
-                if (tv == o.tvp && tu == o.tup) {
-                    pos = b.off[bin] + basep + (unsigned)__popc(peers & lt_mask);
-                } else {
-                    const unsigned tot = b.cnt_prim[bin] + b.cnt_dup[bin];
-                    pos = b.off[bin] + tot - 1u - atomicAdd(&b.cur_dup[bin], 1u);
+    const long long stride = (long long)gridDim.x * blockDim.x * kItems;
+    for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
+        double x[kItems], y[kItems], z[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+            x[i] = m < n ? __ldcs(uu + m) : 0.0;
+            y[i] = m < n ? __ldcs(vv + m) : 0.0;
+            z[i] = m < n ? __ldcs(ww + m) : 0.0;
+        }
+        MGeom o[kItems];
+        S fu[kItems], fv[kItems];
+        int st[kItems];
+        unsigned basep[kItems], peers[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+            fu[i] = fv[i] = 0;
+            st[i] = m < n ? measure<UP2, WP2, S>(g, x[i], y[i], z[i], o[i], fu[i], fv[i]) : 3;
+            const unsigned prim = (st[i] == 0) ? bin_index(g, o[i].gw, o[i].tvp, o[i].tup) : kFull;
+            peers[i] = __match_any_sync(kFull, prim);
+            const int leader = __ffs(peers[i]) - 1;
+            unsigned got = 0;
+            if (st[i] == 0 && lane == leader)
+                got = atomicAdd(&b.cur_prim[prim], (unsigned)__popc(peers[i]));
+            basep[i] = __shfl_sync(kFull, got, leader);
+        }
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+            if (st[i] != 0) continue;
+            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+            S re, im;
+            fold_value<S>(vr, vi, wt, m, nf, np, re, im);
+            for (int tv = o[i].tv0; tv <= o[i].tv1; tv++) {
+                for (int tu = o[i].tu0; tu <= o[i].tu1; tu++) {
+                    const unsigned bin = bin_index(g, o[i].gw, tv, tu);
+                    unsigned pos;
+                    if (tv == o[i].tvp && tu == o[i].tup) {
+                        pos = b.off[bin] + basep[i] + (unsigned)__popc(peers[i] & lt_mask);
+                    } else {
+                        const unsigned tot = b.cnt_prim[bin] + b.cnt_dup[bin];
+                        pos = b.off[bin] + tot - 1u - atomicAdd(&b.cur_dup[bin], 1u);
+                    }
+                    const int cu = o[i].gu - tu * g.tile;
+                    const int cv = o[i].gv - tv * g.tile;
+                    if (PREC == WSG_FP64) {
+                        r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
+                        reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu[i], fv[i]);
+                        reinterpret_cast<double2 *>(r.val)[pos] = make_double2(re, im);
+                    } else {
+                        r.rec16[pos] = make_uint4(pack_axis(cu, (float)fu[i]),
+                                                  pack_axis(cv, (float)fv[i]),
+                                                  __float_as_uint((float)re),
+                                                  __float_as_uint((float)im));
+                    }
+                    r.idx[pos] = (unsigned)m;
                 }
-                const int cu = o.gu - tu * g.tile;
-                const int cv = o.gv - tv * g.tile;
-                r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
-                frac[pos] = fr;
-                val[pos] = vv2;
-                r.idx[pos] = (unsigned)m;
             }
         }
     }
 }
 
-// Single-CTA exclusive scan of the bin sizes and a longest-first bin order
-// (bins bucketed by floor(log2(size)), largest bucket first) for the
-// persistent tile kernels.
-__global__ void __launch_bounds__(1024) k_bin_scan(long long nbins, BinBuffers b)
+// ---- scan of the bin sizes and the work decomposition ----------------------
+
+__device__ __forceinline__ unsigned split_items(unsigned t, unsigned split)
 {
-    __shared__ unsigned long long s_warp[32];
-    __shared__ unsigned s_hist[33];
-    __shared__ unsigned s_cur[33];
+    return t > split ? (t + split - 1) / split : 0u;
+}
+
+// per-CTA partials: part[2*blk] = records, part[2*blk+1] = items | slots << 32
+__global__ void __launch_bounds__(kScanThreads) k_bin_scan_a(long long nbins, BinBuffers b)
+{
+    __shared__ unsigned long long s_rec[kScanThreads / 32], s_pk[kScanThreads / 32];
     __shared__ unsigned s_max;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid < 33) s_hist[tid] = 0;
     if (tid == 0) s_max = 0;
     __syncthreads();
-    const long long per = (nbins + 1023) / 1024;
-    const long long beg = min((long long)tid * per, nbins);
-    const long long end = min(beg + per, nbins);
-    unsigned long long local = 0;
+    const long long beg = (long long)blockIdx.x * kScanPerBlock;
+    unsigned long long rec = 0, pk = 0;
     unsigned lmax = 0;
-    for (long long i = beg; i < end; i++) {
-        const unsigned t = b.cnt_prim[i] + b.cnt_dup[i];
-        local += t;
-        lmax = max(lmax, t);
-        atomicAdd(&s_hist[t ? 32 - __clz(t) : 0], 1u);
+    for (int k = 0; k < kScanPerBlock / kScanThreads; k++) {
+        const long long i = beg + (long long)k * kScanThreads + tid;
+        if (i < nbins) {
+            const unsigned t = b.cnt_prim[i] + b.cnt_dup[i];
+            const unsigned it = split_items(t, b.split_size);
+            rec += t;
+            pk += (unsigned long long)it | ((unsigned long long)(it ? it - 1 : 0) << 32);
+            lmax = max(lmax, t);
+        }
     }
-    // block-wide exclusive scan of `local`
-    unsigned long long incl = local;
-    for (int d = 1; d < 32; d <<= 1) {
-        const unsigned long long v = __shfl_up_sync(kFull, incl, d);
-        if (lane >= d) incl += v;
+    for (int d = 16; d >= 1; d >>= 1) {
+        rec += __shfl_xor_sync(kFull, rec, d);
+        pk += __shfl_xor_sync(kFull, pk, d);
     }
-    if (lane == 31) s_warp[warp] = incl;
+    if (lane == 0) {
+        s_rec[warp] = rec;
+        s_pk[warp] = pk;
+    }
     atomicMax(&s_max, lmax);
     __syncthreads();
-    if (warp == 0) {
-        unsigned long long w = s_warp[lane];
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned long long v = __shfl_up_sync(kFull, w, d);
-            if (lane >= d) w += v;
+    if (tid == 0) {
+        unsigned long long r = 0, q = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) {
+            r += s_rec[w];
+            q += s_pk[w];
         }
-        s_warp[lane] = w;  // inclusive warp prefix
+        b.part[2 * blockIdx.x] = r;
+        b.part[2 * blockIdx.x + 1] = q;
+        atomicMax(&b.ctr->max_bin, s_max);
     }
+}
+
+// One CTA: exclusive scan of the per-CTA partials (both words).
+__global__ void __launch_bounds__(1024) k_bin_scan_b(int nblk, BinBuffers b)
+{
+    __shared__ unsigned long long s_w0[32], s_w1[32];
+    __shared__ unsigned long long s_c0, s_c1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_c0 = s_c1 = 0;
     __syncthreads();
-    unsigned long long run = incl - local + (warp ? s_warp[warp - 1] : 0ull);
-    for (long long i = beg; i < end; i++) {
-        b.off[i] = (unsigned)run;
-        run += b.cnt_prim[i] + b.cnt_dup[i];
+    for (int c0 = 0; c0 < nblk; c0 += 1024) {
+        const int i = c0 + tid;
+        const unsigned long long v0 = i < nblk ? b.part[2 * i] : 0ull;
+        const unsigned long long v1 = i < nblk ? b.part[2 * i + 1] : 0ull;
+        unsigned long long a0 = v0, a1 = v1;
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long t0 = __shfl_up_sync(kFull, a0, d);
+            const unsigned long long t1 = __shfl_up_sync(kFull, a1, d);
+            if (lane >= d) {
+                a0 += t0;
+                a1 += t1;
+            }
+        }
+        if (lane == 31) {
+            s_w0[warp] = a0;
+            s_w1[warp] = a1;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w0 = s_w0[lane], w1 = s_w1[lane];
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long t0 = __shfl_up_sync(kFull, w0, d);
+                const unsigned long long t1 = __shfl_up_sync(kFull, w1, d);
+                if (lane >= d) {
+                    w0 += t0;
+                    w1 += t1;
+                }
+            }
+            s_w0[lane] = w0;
+            s_w1[lane] = w1;
+        }
+        __syncthreads();
+        if (i < nblk) {
+            b.part[2 * i] = s_c0 + a0 - v0 + (warp ? s_w0[warp - 1] : 0ull);
+            b.part[2 * i + 1] = s_c1 + a1 - v1 + (warp ? s_w1[warp - 1] : 0ull);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_c0 += s_w0[31];
+            s_c1 += s_w1[31];
+        }
+        __syncthreads();
     }
     if (tid == 0) {
-        unsigned acc = 0;
-        for (int c = 32; c >= 0; c--) {
-            s_cur[c] = acc;
-            acc += s_hist[c];
+        b.ctr->records = s_c0;
+        b.ctr->nsplit_items = (unsigned)(s_c1 & 0xFFFFFFFFull);
+        b.ctr->nslots = (unsigned)(s_c1 >> 32);
+    }
+}
+
+// Per bin: record offset, split flag, first partial-tile slot, split items.
+__global__ void __launch_bounds__(kScanThreads) k_bin_scan_c(long long nbins, BinBuffers b)
+{
+    __shared__ unsigned long long s_w0[kScanThreads / 32], s_w1[kScanThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long beg = (long long)blockIdx.x * kScanPerBlock;
+    constexpr int PER = kScanPerBlock / kScanThreads;   // consecutive bins per thread
+    unsigned long long l0 = 0, l1 = 0;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        const long long i = beg + (long long)tid * PER + k;
+        const unsigned t = i < nbins ? b.cnt_prim[i] + b.cnt_dup[i] : 0u;
+        const unsigned it = split_items(t, b.split_size);
+        l0 += t;
+        l1 += (unsigned long long)it | ((unsigned long long)(it ? it - 1 : 0) << 32);
+    }
+    unsigned long long a0 = l0, a1 = l1;
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long t0 = __shfl_up_sync(kFull, a0, d);
+        const unsigned long long t1 = __shfl_up_sync(kFull, a1, d);
+        if (lane >= d) {
+            a0 += t0;
+            a1 += t1;
         }
-        b.ctr->records = s_warp[31];
-        b.ctr->max_bin = s_max;
+    }
+    if (lane == 31) {
+        s_w0[warp] = a0;
+        s_w1[warp] = a1;
     }
     __syncthreads();
-    for (long long i = beg; i < end; i++) {
+    if (warp == 0) {
+        unsigned long long w0 = lane < kScanThreads / 32 ? s_w0[lane] : 0ull;
+        unsigned long long w1 = lane < kScanThreads / 32 ? s_w1[lane] : 0ull;
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long t0 = __shfl_up_sync(kFull, w0, d);
+            const unsigned long long t1 = __shfl_up_sync(kFull, w1, d);
+            if (lane >= d) {
+                w0 += t0;
+                w1 += t1;
+            }
+        }
+        if (lane < kScanThreads / 32) {
+            s_w0[lane] = w0;
+            s_w1[lane] = w1;
+        }
+    }
+    __syncthreads();
+    unsigned long long r0 = b.part[2 * blockIdx.x] + a0 - l0 + (warp ? s_w0[warp - 1] : 0ull);
+    unsigned long long r1 = b.part[2 * blockIdx.x + 1] + a1 - l1 + (warp ? s_w1[warp - 1] : 0ull);
+    for (int k = 0; k < PER; k++) {
+        const long long i = beg + (long long)tid * PER + k;
+        if (i >= nbins) break;
         const unsigned t = b.cnt_prim[i] + b.cnt_dup[i];
-        const unsigned pos = atomicAdd(&s_cur[t ? 32 - __clz(t) : 0], 1u);
-        b.order[pos] = (unsigned)i;
+        const unsigned it = split_items(t, b.split_size);
+        b.off[i] = (unsigned)r0;
+        b.is_split[i] = it ? 1u : 0u;
+        b.slot[i] = (unsigned)(r1 >> 32);
+        b.done[i] = 0u;
+        const unsigned first = (unsigned)(r1 & 0xFFFFFFFFull);
+        for (unsigned c = 0; c < it; c++)
+            b.split[first + c] = (unsigned long long)i | ((unsigned long long)c << 32);
+        r0 += t;
+        r1 += (unsigned long long)it | ((unsigned long long)(it ? it - 1 : 0) << 32);
     }
 }
 
 int stream_grid(long long n, int threads)
 {
-    const long long want = (n + threads - 1) / threads;
+    const long long want = (n + (long long)threads * kItems - 1) / ((long long)threads * kItems);
     const long long cap = (long long)num_sms() * 8;
     return (int)max(1ll, min(want, cap));
 }
 
 }  // namespace
+
+long long scan_blocks(long long nbins) { return (nbins + kScanPerBlock - 1) / kScanPerBlock; }
 
 cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double *vv,
                              const double *ww, long long n, const BinBuffers &b, cudaStream_t s)
@@ -271,11 +424,14 @@ cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double
 
 cudaError_t launch_bin_scan(const GeomParams &g, const BinBuffers &b, cudaStream_t s)
 {
-    k_bin_scan<<<1, 1024, 0, s>>>(g.nbins, b);
+    const long long nblk = scan_blocks(g.nbins);
+    k_bin_scan_a<<<(unsigned)nblk, kScanThreads, 0, s>>>(g.nbins, b);
+    k_bin_scan_b<<<1, 1024, 0, s>>>((int)nblk, b);
+    k_bin_scan_c<<<(unsigned)nblk, kScanThreads, 0, s>>>(g.nbins, b);
     return cudaGetLastError();
 }
 
-template <typename F2>
+template <int PREC>
 static void scatter_dispatch(const GeomParams &g, const double *uu, const double *vv,
                              const double *ww, const float *vr, const float *vi,
                              const float *wt, long long n, long long nf, long long np,
@@ -283,13 +439,13 @@ static void scatter_dispatch(const GeomParams &g, const double *uu, const double
 {
     const int blocks = stream_grid(n, 256);
     if (g.u_pow2 && g.w_pow2)
-        k_bin_scatter<true, true, F2><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<true, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
     else if (g.u_pow2)
-        k_bin_scatter<true, false, F2><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<true, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
     else if (g.w_pow2)
-        k_bin_scatter<false, true, F2><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<false, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
     else
-        k_bin_scatter<false, false, F2><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<false, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
 }
 
 cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu, const double *vv,
@@ -298,8 +454,8 @@ cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu, 
                                const BinBuffers &b, const RecBuffers &r, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    if (prec == WSG_FP64) scatter_dispatch<double2>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r, s);
-    else scatter_dispatch<float2>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r, s);
+    if (prec == WSG_FP64) scatter_dispatch<WSG_FP64>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r, s);
+    else scatter_dispatch<WSG_FP32C>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r, s);
     return cudaGetLastError();
 }
 

@@ -141,13 +141,14 @@ struct wsg_plan {
     int nx, ny, planes, support, half, prec;
     double dx, dw;
     cudaStream_t stream = nullptr;
-    int tile = 64, ctas_grid = 0, ctas_degrid = 0, chunk = 2048, ctas_user = 0;
+    int tile = 64, ctas_grid = 0, ctas_degrid = 0, split = kDefaultSplit, ctas_user = 0;
     GeomParams geom{};
 
     DevBuf grid;                          // resident [P][Ny][Nx] complex
-    DevBuf bins;                          // 6 x nbins u32
+    DevBuf bins;                          // bin_buffer_bytes(nbins)
     DevBuf ctr;                           // DevCounters
-    DevBuf rcell, rfrac, rval, ridx;      // records
+    DevBuf rec16, rcell, rfrac, rval, ridx;   // records (FP32C: rec16+idx; FP64: SoA)
+    DevBuf partials;                      // FP32C partial tiles of split bins
     unsigned long long rec_cap = 0;
     long long n_binned = -1;
 
@@ -168,20 +169,15 @@ struct wsg_plan {
     BinBuffers binbufs() const
     {
         BinBuffers b;
-        unsigned *base = bins.as<unsigned>();
-        const long long nb = geom.nbins;
-        b.cnt_prim = base;
-        b.cnt_dup = base + nb;
-        b.cur_prim = base + 2 * nb;
-        b.cur_dup = base + 3 * nb;
-        b.off = base + 4 * nb;
-        b.order = base + 5 * nb;
+        bin_buffer_carve(bins.p, geom.nbins, b);
         b.ctr = ctr.as<DevCounters>();
+        b.split_size = (unsigned)split;
         return b;
     }
     RecBuffers recbufs() const
     {
         RecBuffers r;
+        r.rec16 = rec16.as<uint4>();
         r.cell = rcell.as<unsigned>();
         r.frac = rfrac.p;
         r.val = rval.p;
@@ -236,7 +232,7 @@ int plan_configure(wsg_plan *p)
                          p->support);
     p->ctas_grid = p->ctas_user > 0 ? p->ctas_user : og * sms;
     p->ctas_degrid = p->ctas_user > 0 ? p->ctas_user : od * sms;
-    WSG_CUDA(p->bins.ensure((size_t)6 * g.nbins * sizeof(unsigned)));
+    p->rec_cap = 0;  // bin table and partial-tile sizes depend on tile and split
     p->n_binned = -1;
     return WSG_OK;
 }
@@ -246,11 +242,18 @@ int ensure_records(wsg_plan *p, long long n)
     // a support window of <= tile cells touches at most 2x2 tiles
     const unsigned long long need = (unsigned long long)(n > 0 ? n : 1) * 4ull;
     if (need <= p->rec_cap) return WSG_OK;
-    const size_t fsz = p->prec == WSG_FP64 ? sizeof(double2) : sizeof(float2);
-    WSG_CUDA(p->rcell.ensure(need * sizeof(unsigned)));
+    WSG_CUDA(p->bins.ensure(bin_buffer_bytes(p->geom.nbins, max_split_items(need, p->split))));
+    if (p->prec == WSG_FP32C)
+        WSG_CUDA(p->partials.ensure(max_slots(need, p->split) * (size_t)p->tile * p->tile *
+                                    sizeof(float2)));
     WSG_CUDA(p->ridx.ensure(need * sizeof(unsigned)));
-    WSG_CUDA(p->rfrac.ensure(need * fsz));
-    WSG_CUDA(p->rval.ensure(need * fsz));
+    if (p->prec == WSG_FP64) {
+        WSG_CUDA(p->rcell.ensure(need * sizeof(unsigned)));
+        WSG_CUDA(p->rfrac.ensure(need * sizeof(double2)));
+        WSG_CUDA(p->rval.ensure(need * sizeof(double2)));
+    } else {
+        WSG_CUDA(p->rec16.ensure(need * sizeof(uint4)));
+    }
     p->rec_cap = need;
     return WSG_OK;
 }
@@ -351,7 +354,7 @@ int wsg_plan_destroy(wsg_plan *p)
 {
     if (!p) return WSG_OK;
     if (p->fft) cufftDestroy(p->fft);
-    DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rcell, &p->rfrac, &p->rval, &p->ridx,
+    DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rec16, &p->partials, &p->rcell, &p->rfrac, &p->rval, &p->ridx,
                       &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi, &p->h_wt, &p->h_image,
                       &p->h_out, &p->sinx, &p->siny, &p->wscreen, &p->fft_work};
     for (DevBuf *b : bufs) b->release();
@@ -376,7 +379,9 @@ int wsg_plan_set_tuning(wsg_plan *p, int tile, int ctas, int chunk)
     if (tile && 2 * p->half + 1 > tile)
         return set_error(WSG_ERR_UNSUPPORTED, "tile smaller than the support");
     if (chunk < 0 || ctas < 0) return set_error(WSG_ERR_ARG, "negative tuning value");
-    if (chunk > 0) p->chunk = chunk;
+    if (chunk > 0 && chunk < kStage)
+        return set_error(WSG_ERR_UNSUPPORTED, "split size below %d records", kStage);
+    if (chunk > 0) p->split = chunk;
     p->ctas_user = ctas;
     if (tile) p->tile = tile;
     return plan_configure(p);
@@ -435,7 +440,7 @@ int wsg_plan_get_stats(wsg_plan *p, wsg_stats *s)
 long long wsg_plan_device_bytes(wsg_plan *p)
 {
     if (!p) return 0;
-    const DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rcell, &p->rfrac, &p->rval,
+    const DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rec16, &p->partials, &p->rcell, &p->rfrac, &p->rval,
                             &p->ridx, &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi,
                             &p->h_wt, &p->h_image, &p->h_out, &p->sinx, &p->siny,
                             &p->wscreen, &p->fft_work};
@@ -474,7 +479,7 @@ int wsg_grid(wsg_plan *p, void *grid)
     if (p->n_binned < 0) return set_error(WSG_ERR_STATE, "wsg_grid before wsg_bin");
     const BinBuffers b = p->binbufs();
     WSG_CUDA(cudaMemsetAsync(&b.ctr->work_grid, 0, sizeof(unsigned), p->stream));
-    WSG_CUDA(launch_grid(p->geom, p->prec, b, p->recbufs(), grid, p->ctas_grid, p->chunk,
+    WSG_CUDA(launch_grid(p->geom, p->prec, b, p->recbufs(), grid, p->partials.p, p->ctas_grid,
                          p->stream));
     return WSG_OK;
 }

@@ -6,11 +6,15 @@
 // exactly the transpose of the map V_m -> grid of w-stacking.cu:59-117.
 //
 // It reuses the gridder's sort: a persistent CTA takes a (plane, tile) bin,
-// stages the tile plus its K-cell halo from HBM into shared memory once
-// (cells off the grid read as zero), then each warp gathers one primary
-// measurement: lanes take taps, a shuffle tree sums them, lane 0 stores the
-// complex result at the measurement's original index.  Duplicate records of
-// the bin are not visited: the halo makes every primary's window local.
+// stages the tile plus a halo from HBM into shared memory once (cells off the
+// grid read as zero), then gathers the bin's primary records.  Duplicate
+// records of the bin are not visited: the halo makes every primary's window
+// local.
+//   FP32C: records staged kStage at a time; a group of 8 (or 16) lanes takes
+//   one record, lane k its row k: the row sum over the NT columns uses the
+//   column weights shuffled from the group's lanes, the row weight is applied
+//   once, and a shuffle tree over the group sums the rows.
+//   FP64: a warp takes one record, lanes take taps, a shuffle tree sums them.
 #include <cuda_runtime.h>
 
 #include "wsg_internal.cuh"
@@ -51,6 +55,120 @@ template <> struct Cx<double2> {
 __device__ __forceinline__ float gauss1d(float d) { return __expf(-0.5f * (d * d)); }
 __device__ __forceinline__ double gauss1d(double d) { return exp(-(d * d) * 0.5); }
 
+// Work item -> (bin, primaries [p0, p1)); the same items as the gridder.
+__device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, unsigned nsplit,
+                                            unsigned &bin, unsigned &p0, unsigned &p1)
+{
+    unsigned chunk = 0;
+    if (item < nsplit) {
+        const unsigned long long e = b.split[item];
+        bin = (unsigned)(e & 0xFFFFFFFFull);
+        chunk = (unsigned)(e >> 32);
+    } else {
+        bin = item - nsplit;
+        if (b.is_split[bin]) return false;
+    }
+    const unsigned nprim = b.cnt_prim[bin];
+    if (item < nsplit) {
+        p0 = min(nprim, chunk * b.split_size);
+        p1 = min(nprim, p0 + b.split_size);
+    } else {
+        p0 = 0;
+        p1 = nprim;
+    }
+    return p1 > p0;
+}
+
+template <int T, int K>
+__global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
+{
+    constexpr int NT = 2 * K + 1;
+    constexpr int GS = NT <= 8 ? 8 : 16;   // lanes per record (power of two)
+    constexpr int RPW = 32 / GS;
+    constexpr int H = 2 * K;
+    constexpr int AW = T + 2 * H;
+    constexpr int AP = AW | 1;
+    constexpr int NW = kThreads / 32;
+    constexpr int TB = (AW * AP * 8 + 15) / 16 * 16;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2 *tile = reinterpret_cast<float2 *>(smraw);
+    uint4 *stage = reinterpret_cast<uint4 *>(smraw + TB);
+    unsigned *sidx = reinterpret_cast<unsigned *>(smraw + TB + kStage * sizeof(uint4));
+    __shared__ unsigned s_item;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int grp = lane / GS, k = lane % GS;
+    const bool on = k < NT;
+    const int kk = on ? k : NT - 1;
+    const float norm = (float)(0.5 / kRefPi);
+    const float c2 = -0.72134752044448170368f;   // -0.5 * log2(e)
+    const float off1 = (float)(kk - K) + 0.5f;
+    const float2 *__restrict__ grid = reinterpret_cast<const float2 *>(a.grid);
+    float2 *out = reinterpret_cast<float2 *>(a.out);
+    const unsigned nsplit = a.b.ctr->nsplit_items;
+    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_degrid, 1u);
+        __syncthreads();
+        const unsigned item = s_item;
+        if (item >= nitems) break;
+        unsigned bin, p0, p1;
+        if (!work_item_d(a.b, item, nsplit, bin, p0, p1)) continue;
+        int w, u0, v0;
+        decode_bin_d(a.g, bin, w, u0, v0);
+        const unsigned off = a.b.off[bin];
+        const size_t plane = (size_t)w * a.g.ny;
+        for (int i = tid; i < AW * AW; i += kThreads) {
+            const int y = i / AW, x = i - (i / AW) * AW;
+            const int gy = v0 - H + y, gx = u0 - H + x;
+            float2 val = make_float2(0.f, 0.f);
+            if (gx >= 0 && gx < a.g.nx && gy >= 0 && gy < a.g.ny)
+                val = grid[(plane + (size_t)gy) * a.g.nx + (size_t)gx];
+            tile[y * AP + x] = val;
+        }
+        for (unsigned c0 = p0; c0 < p1; c0 += kStage) {
+            const unsigned cnt = min((unsigned)kStage, p1 - c0);
+            __syncthreads();
+            for (unsigned i = tid; i < cnt; i += kThreads) {
+                stage[i] = __ldcs(a.r.rec16 + off + c0 + i);
+                sidx[i] = __ldcs(a.r.idx + off + c0 + i);
+            }
+            __syncthreads();
+            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
+                const unsigned r = base + grp;
+                const bool valid = r < cnt;
+                const uint4 q = stage[valid ? r : 0];
+                const int cu = (int)(q.x >> 24) - 64;
+                const int cv = (int)(q.y >> 24) - 64;
+                const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float du = off1 - fu, dv = off1 - fv;
+                const float gu = norm * exp2f(du * du * c2);
+                const float gv = on ? exp2f(dv * dv * c2) : 0.0f;
+                const int row = (cv - K + kk + H) * AP + (cu - K + H);
+                float sr = 0.f, si = 0.f;
+#pragma unroll
+                for (int j = 0; j < NT; j++) {
+                    const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * GS + j);
+                    const float2 t = tile[row + j];
+                    sr = fmaf(g, t.x, sr);
+                    si = fmaf(g, t.y, si);
+                }
+                sr *= gv;
+                si *= gv;
+#pragma unroll
+                for (int d = GS / 2; d >= 1; d >>= 1) {
+                    sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
+                    si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
+                }
+                if (k == 0 && valid) out[sidx[r]] = make_float2(sr, si);
+            }
+        }
+    }
+}
+
 template <int T, int K, typename C2>
 __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
 {
@@ -70,6 +188,8 @@ __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
     const C2 *__restrict__ grid = reinterpret_cast<const C2 *>(a.grid);
     const C2 *__restrict__ fr_all = reinterpret_cast<const C2 *>(a.r.frac);
     C2 *out = reinterpret_cast<C2 *>(a.out);
+    const unsigned nsplit = a.b.ctr->nsplit_items;
+    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
 
     int odj[ROUNDS], odk[ROUNDS];
 #pragma unroll
@@ -87,10 +207,9 @@ __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
         if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_degrid, 1u);
         __syncthreads();
         const unsigned item = s_item;
-        if ((long long)item >= a.g.nbins) break;
-        const unsigned bin = a.b.order[item];
-        const unsigned nprim = a.b.cnt_prim[bin];
-        if (nprim == 0) continue;
+        if (item >= nitems) break;
+        unsigned bin, p0, p1;
+        if (!work_item_d(a.b, item, nsplit, bin, p0, p1)) continue;
         int w, u0, v0;
         decode_bin_d(a.g, bin, w, u0, v0);
         const unsigned off = a.b.off[bin];
@@ -104,7 +223,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
             tile[y * SP + x] = val;
         }
         __syncthreads();
-        for (unsigned rr = warp; rr < nprim; rr += NW) {
+        for (unsigned rr = p0 + warp; rr < p1; rr += NW) {
             const unsigned cell = __ldg(a.r.cell + off + rr);
             const C2 fr = fr_all[off + rr];
             const unsigned idx = __ldg(a.r.idx + off + rr);
@@ -147,14 +266,16 @@ __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
 
 template <int T, int K> size_t degrid_smem(int prec)
 {
-    return (size_t)(T + 2 * K) * (T + 2 * K + 1) *
-           (prec == WSG_FP64 ? sizeof(double2) : sizeof(float2));
+    if (prec == WSG_FP64) return (size_t)(T + 2 * K) * (T + 2 * K + 1) * sizeof(double2);
+    constexpr int AW = T + 4 * K;
+    constexpr int AP = AW | 1;
+    return ((size_t)AW * AP * 8 + 15) / 16 * 16 + (size_t)kStage * (sizeof(uint4) + sizeof(unsigned));
 }
 
 template <int T, int K> const void *degrid_kernel(int prec)
 {
     return prec == WSG_FP64 ? (const void *)k_degrid<T, K, double2>
-                            : (const void *)k_degrid<T, K, float2>;
+                            : (const void *)k_degrid_f32c<T, K>;
 }
 
 template <int T>

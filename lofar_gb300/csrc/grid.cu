@@ -1,26 +1,26 @@
-// Gridding kernels: one persistent CTA per SM slot walks the (plane, tile)
-// bins longest-first and accumulates each tile in shared memory, then writes
-// it to HBM once with coalesced stores.  Every cell of the grid belongs to
-// exactly one tile, and measurements near a tile edge were duplicated into
-// the neighbouring bins by the binning pass, so tiles are written with plain
-// stores: no global atomics, no memset of the grid.
+// Gridding kernels.  Persistent CTAs take work items from a queue: first the
+// items of split bins (bins with more than `split` records, cut into items of
+// at most `split` records), then every other (plane, tile) bin.  Each item is
+// accumulated in shared memory and its T x T interior written to HBM once with
+// coalesced stores.  Every grid cell belongs to exactly one tile, and
+// measurements near a tile edge were duplicated into the neighbouring bins by
+// the binning pass, so tiles are written with plain stores: no global
+// atomics, no memset of the grid.  This replaces convolve_g
+// (w-stacking.cu:35-118), whose FP64 global atomics scatter every tap to HBM.
 //
-// Work inside a tile (replaces convolve_g, w-stacking.cu:35-118, whose FP64
-// global atomics scatter each tap to HBM): a warp takes one measurement and
-// its lanes take the (2K+1)^2 taps of the support window.  The tile's
-// shared-memory pitch is T + 2K + 1, congruent to the window width modulo 32,
-// so the taps of one window fall in distinct banks: the tap scatter is
-// conflict-free.
+// FP32C (k_grid_f32c): see the kernel's comment for the lane layout and the
+// fixed-point tile accumulator.  An item of a split bin writes its partial
+// tile (chunk 0 straight into the grid, the others into partial-tile slots);
+// the CTA that finishes a split bin's last item combines the bin's partials
+// cell by cell with TwoSum (hi + lo), in chunk order, so the error of a cell
+// does not grow with the number of measurements that hit it.
 //
-// FP32C: taps are added with shared-memory float atomics into an FP32
-// chunk accumulator; after every `chunk` measurements each thread folds the
-// cells it owns into a register-resident two-float (hi + lo, TwoSum) master
-// tile and clears them.  The grid therefore carries compensated sums whose
-// error does not grow with the number of measurements in a cell.
-//
-// FP64: taps are added with FP64 shared-memory atomics; the separable
-// Gaussian exp(-du^2/2)*exp(-dv^2/2) is evaluated once per row/column
-// (2(2K+1) FP64 exponentials per measurement instead of (2K+1)^2).
+// FP64 (k_grid_f64): whole bins (a split bin is processed by the CTA that
+// takes its first item); a warp takes one record and its lanes the
+// (2K+1)^2 taps; the tile's pitch T + 2K + 1 is congruent to the window
+// width modulo 16 doubles, so the taps of one window fall in distinct banks.
+// FP64 shared-memory atomics; the separable Gaussian
+// exp(-du^2/2)*exp(-dv^2/2) costs 2(2K+1) FP64 exponentials per record.
 #include <cuda_runtime.h>
 
 #include "wsg_internal.cuh"
@@ -34,7 +34,7 @@ struct GridArgs {
     BinBuffers b;
     RecBuffers r;
     void *grid;
-    int chunk;
+    void *partials;
 };
 
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
@@ -57,99 +57,209 @@ __device__ __forceinline__ void decode_bin(const GeomParams &g, unsigned bin, in
     v0 = tv * g.tile;
 }
 
+// Work item -> (bin, chunk).  Returns false for a bin that is handled by
+// split items instead.
+__device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, unsigned nsplit,
+                                          unsigned &bin, unsigned &chunk)
+{
+    if (item < nsplit) {
+        const unsigned long long e = b.split[item];
+        bin = (unsigned)(e & 0xFFFFFFFFull);
+        chunk = (unsigned)(e >> 32);
+        return true;
+    }
+    bin = item - nsplit;
+    chunk = 0;
+    return b.is_split[bin] == 0u;
+}
+
+// FP32C tile kernel.  A warp pass takes RPW = 32/NT records; lane (g, k) of
+// record g owns row k of its support window: it evaluates the column weight
+// gu_k and the row weight gv_k of the separable Gaussian once, then walks the
+// NT columns of its row, fetching gu_j from lane (g, j) with a shuffle and
+// adding V*gv_k*gu_j into the shared-memory accumulator (odd pitch: the NT
+// rows of one record fall in distinct banks).  Records are staged into shared
+// memory kStage at a time with coalesced 16-byte loads.
+//
+// The accumulator is int32 fixed point: shared-memory integer atomics retire
+// about five times faster than float ones on this part.  Each work item first
+// bounds its largest cell from the local sums of |Re V| + |Im V| (see below)
+// and picks the scale 2^f that keeps every cell sum below 2^30, with room for
+// the rounding of each term.  The integer sums are exact and
+// order-independent; the only error is the rounding of each tap to the
+// item's quantum, 2^-f.
+//
+// The accumulator has a 2K halo on every side so that every tap of every
+// record of the bin lands in it without a bounds test; the halo is never read
+// and is not cleared (it only collects the taps of neighbouring tiles).
 template <int T, int K>
-__global__ void __launch_bounds__(kThreads) k_grid_f32c(GridArgs a)
+__global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
 {
     constexpr int NT = 2 * K + 1;
-    constexpr int NTAP = NT * NT;
-    constexpr int ROUNDS = (NTAP + 31) / 32;
-    constexpr int PITCH = T + NT;
+    constexpr int RPW = 32 / NT;
+    constexpr int H = 2 * K;
+    constexpr int AW = T + 2 * H;
+    constexpr int AP = AW | 1;
     constexpr int NW = kThreads / 32;
     constexpr int CPT = T * T / kThreads;
-    extern __shared__ float sm[];
-    float *sre = sm;
-    float *sim = sm + T * PITCH;
+    constexpr int ACC = ((2 * AW * AP * 4) + 15) / 16 * 16;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    int *are = reinterpret_cast<int *>(smraw);
+    int *aim = are + AW * AP;
+    uint4 *stage = reinterpret_cast<uint4 *>(smraw + ACC);
     __shared__ unsigned s_item;
+    __shared__ int s_last;
+    constexpr int NB = (AW + 7) / 8;   // 8x8-cell blocks of the accumulator
+    __shared__ float s_part[NW];
+    __shared__ float s_blk[NB * NB];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int grp = lane / NT, k = lane - (lane / NT) * NT;
+    const bool lane_on = grp < RPW;
     const float norm = (float)(0.5 / kRefPi);
-    const float2 *__restrict__ fr_all = reinterpret_cast<const float2 *>(a.r.frac);
-    const float2 *__restrict__ val_all = reinterpret_cast<const float2 *>(a.r.val);
+    const float c2 = -0.72134752044448170368f;   // -0.5 * log2(e)
+    const float off1 = (float)(k - K) + 0.5f;
+    const uint4 *__restrict__ rec = a.r.rec16;
     float2 *grid = reinterpret_cast<float2 *>(a.grid);
+    float2 *parts = reinterpret_cast<float2 *>(a.partials);
+    const unsigned nsplit = a.b.ctr->nsplit_items;
+    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+    const unsigned split = a.b.split_size;
 
-    int odj[ROUNDS], odk[ROUNDS];
-    float offu[ROUNDS], offv[ROUNDS];
-#pragma unroll
-    for (int r = 0; r < ROUNDS; r++) {
-        const int l = lane + 32 * r;
-        odk[r] = (l < NTAP) ? l / NT : 4096;
-        odj[r] = l % NT;
-        offu[r] = (float)(odj[r] - K) + 0.5f;
-        offv[r] = (float)(odk[r] - K) + 0.5f;
-    }
-    for (int i = tid; i < 2 * T * PITCH; i += kThreads) sm[i] = 0.0f;
+    for (int i = tid; i < 2 * AW * AP; i += kThreads) are[i] = 0;
 
     for (;;) {
         __syncthreads();
         if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_grid, 1u);
         __syncthreads();
         const unsigned item = s_item;
-        if ((long long)item >= a.g.nbins) break;
-        const unsigned bin = a.b.order[item];
+        if (item >= nitems) break;
+        unsigned bin, chunk;
+        if (!work_item(a.b, item, nsplit, bin, chunk)) continue;
         int w, u0, v0;
         decode_bin(a.g, bin, w, u0, v0);
         const int tx = min(T, a.g.nx - u0);
         const int ty = min(T, a.g.ny - v0);
+        const unsigned total = a.b.cnt_prim[bin] + a.b.cnt_dup[bin];
+        const bool is_split = item < nsplit;
+        const unsigned r0 = chunk * split;
+        const unsigned r1 = is_split ? min(total, r0 + split) : total;
         const unsigned off = a.b.off[bin];
-        const unsigned n = a.b.cnt_prim[bin] + a.b.cnt_dup[bin];
 
-        float mhr[CPT], mlr[CPT], mhi[CPT], mli[CPT];
+        // The item's scale.  Sum |Re V| + |Im V| of the records per 8x8 block
+        // of the accumulator (by centre cell); a cell's taps all come from
+        // records centred within K <= 7 cells, i.e. in its block or the 8
+        // around it, so the largest 3x3-block sum times the peak weight norm
+        // bounds every cell of the item.
+        for (int i = tid; i < NB * NB; i += kThreads) s_blk[i] = 0.0f;
+        __syncthreads();
+        for (unsigned i = r0 + tid; i < r1; i += kThreads) {
+            const uint4 q = __ldcg(rec + off + i);
+            const int bx = ((int)(q.x >> 24) - 64 + H) >> 3;
+            const int by = ((int)(q.y >> 24) - 64 + H) >> 3;
+            atomicAdd(&s_blk[by * NB + bx],
+                      fabsf(__uint_as_float(q.z)) + fabsf(__uint_as_float(q.w)));
+        }
+        __syncthreads();
+        float bmax = 0.0f;
+        for (int i = tid; i < NB * NB; i += kThreads) {
+            const int by = i / NB, bx = i - (i / NB) * NB;
+            float t = 0.0f;
+            for (int yy = max(by - 1, 0); yy <= min(by + 1, NB - 1); yy++)
+                for (int xx = max(bx - 1, 0); xx <= min(bx + 1, NB - 1); xx++)
+                    t += s_blk[yy * NB + xx];
+            bmax = fmaxf(bmax, t);
+        }
+        for (int d = 16; d >= 1; d >>= 1) bmax = fmaxf(bmax, __shfl_xor_sync(0xFFFFFFFFu, bmax, d));
+        if (lane == 0) s_part[warp] = bmax;
+        __syncthreads();
+        float bound = 0.0f;
 #pragma unroll
-        for (int i = 0; i < CPT; i++) mhr[i] = mlr[i] = mhi[i] = mli[i] = 0.0f;
+        for (int i = 0; i < NW; i++) bound = fmaxf(bound, s_part[i]);
+        // cell sums stay below 2^30 (+ at most one rounding per term)
+        bound = bound * norm * 1.0001f;
+        int fexp = 30;
+        if (bound > 0.0f) {
+            int e2;
+            frexpf(bound, &e2);   // bound < 2^e2
+            fexp = min(30 - e2, 100);
+        }
+        const float scale = ldexpf(1.0f, fexp);
+        const float inv = ldexpf(1.0f, -fexp);
 
-        for (unsigned c0 = 0; c0 < n; c0 += (unsigned)a.chunk) {
-            const unsigned c1 = min(n, c0 + (unsigned)a.chunk);
-            for (unsigned rr = c0 + warp; rr < c1; rr += NW) {
-                const unsigned cell = __ldg(a.r.cell + off + rr);
-                const float2 fr = __ldg(fr_all + off + rr);
-                const float2 v = __ldg(val_all + off + rr);
-                const int cu = (int)(cell & 0xFFFFu) - 32768 - K;
-                const int cv = (int)(cell >> 16) - 32768 - K;
+        for (unsigned c0 = r0; c0 < r1; c0 += kStage) {
+            const unsigned cnt = min((unsigned)kStage, r1 - c0);
+            __syncthreads();
+            for (unsigned i = tid; i < cnt; i += kThreads) stage[i] = __ldcs(rec + off + c0 + i);
+            __syncthreads();
+            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
+                const unsigned r = base + grp;
+                const bool valid = lane_on && r < cnt;
+                const uint4 q = stage[valid ? r : 0];
+                const int cu = (int)(q.x >> 24) - 64;
+                const int cv = (int)(q.y >> 24) - 64;
+                const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float du = off1 - fu, dv = off1 - fv;
+                const float gu = norm * exp2f(du * du * c2);
+                const float gv = exp2f(dv * dv * c2) * scale;
+                const float ar = __uint_as_float(q.z) * gv;
+                const float ai = __uint_as_float(q.w) * gv;
+                const int row = (cv - K + k + H) * AP + (cu - K + H);
 #pragma unroll
-                for (int r = 0; r < ROUNDS; r++) {
-                    const int x = cu + odj[r];
-                    const int y = cv + odk[r];
-                    if ((unsigned)x < (unsigned)tx && (unsigned)y < (unsigned)ty) {
-                        const float du = offu[r] - fr.x;
-                        const float dv = offv[r] - fr.y;
-                        const float wgt = norm * __expf(-0.5f * (du * du + dv * dv));
-                        atomicAdd(sre + y * PITCH + x, wgt * v.x);
-                        atomicAdd(sim + y * PITCH + x, wgt * v.y);
+                for (int j = 0; j < NT; j++) {
+                    const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
+                    if (valid) {
+                        atomicAdd(are + row + j, __float2int_rn(ar * g));
+                        atomicAdd(aim + row + j, __float2int_rn(ai * g));
                     }
                 }
             }
-            __syncthreads();
-#pragma unroll
-            for (int i = 0; i < CPT; i++) {
-                const int c = tid + i * kThreads;
-                const int idx = (c / T) * PITCH + (c % T);
-                const float xr = sre[idx];
-                const float xi = sim[idx];
-                sre[idx] = 0.0f;
-                sim[idx] = 0.0f;
-                two_sum_acc(mhr[i], mlr[i], xr);
-                two_sum_acc(mhi[i], mli[i], xi);
-            }
-            __syncthreads();
         }
-
-#pragma unroll
+        __syncthreads();
+        // write the interior (to the grid, or to this item's partial slot) and clear it
+        const size_t gbase = (size_t)w * a.g.ny;
+        const bool to_grid = !(is_split && chunk > 0);
+        float2 *dst = to_grid ? grid
+                              : parts + (size_t)(a.b.slot[bin] + chunk - 1) * (size_t)(T * T);
+#pragma unroll 4
         for (int i = 0; i < CPT; i++) {
             const int c = tid + i * kThreads;
             const int y = c / T, x = c % T;
-            if (x < tx && y < ty)
-                grid[((size_t)w * a.g.ny + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x)] =
-                    make_float2(mhr[i] + mlr[i], mhi[i] + mli[i]);
+            const int idx = (y + H) * AP + x + H;
+            const float2 v = make_float2((float)are[idx] * inv, (float)aim[idx] * inv);
+            are[idx] = 0;
+            aim[idx] = 0;
+            if (to_grid) {
+                if (x < tx && y < ty)
+                    __stcg(grid + (gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x), v);
+            } else {
+                __stcg(dst + c, v);
+            }
+        }
+        if (!is_split) continue;
+        // split bin: the CTA finishing its last item combines the partials
+        __threadfence();
+        __syncthreads();
+        const unsigned nchunks = (total + split - 1) / split;
+        if (tid == 0) s_last = atomicAdd(&a.b.done[bin], 1u) == nchunks - 1;
+        __syncthreads();
+        if (!s_last) continue;
+        __threadfence();
+        const float2 *src = parts + (size_t)a.b.slot[bin] * (size_t)(T * T);
+        for (int i = 0; i < CPT; i++) {
+            const int c = tid + i * kThreads;
+            const int y = c / T, x = c % T;
+            if (x >= tx || y >= ty) continue;
+            float2 *cell = grid + (gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x);
+            const float2 g0 = __ldcg(cell);
+            float hr = g0.x, lr = 0.f, hi = g0.y, li = 0.f;
+            for (unsigned q = 1; q < nchunks; q++) {
+                const float2 p = __ldcg(src + (size_t)(q - 1) * (size_t)(T * T) + c);
+                two_sum_acc(hr, lr, p.x);
+                two_sum_acc(hi, li, p.y);
+            }
+            __stcg(cell, make_float2(hr + lr, hi + li));
         }
     }
 }
@@ -172,6 +282,8 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
     const double2 *__restrict__ fr_all = reinterpret_cast<const double2 *>(a.r.frac);
     const double2 *__restrict__ val_all = reinterpret_cast<const double2 *>(a.r.val);
     double2 *grid = reinterpret_cast<double2 *>(a.grid);
+    const unsigned nsplit = a.b.ctr->nsplit_items;
+    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
 
     int odj[ROUNDS], odk[ROUNDS];
 #pragma unroll
@@ -192,8 +304,9 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_grid, 1u);
         __syncthreads();
         const unsigned item = s_item;
-        if ((long long)item >= a.g.nbins) break;
-        const unsigned bin = a.b.order[item];
+        if (item >= nitems) break;
+        unsigned bin, chunk;
+        if (!work_item(a.b, item, nsplit, bin, chunk) || chunk != 0) continue;
         int w, u0, v0;
         decode_bin(a.g, bin, w, u0, v0);
         const int tx = min(T, a.g.nx - u0);
@@ -245,7 +358,10 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
 
 template <int T, int K> size_t grid_smem(int prec)
 {
-    return (size_t)2 * T * (T + 2 * K + 1) * (prec == WSG_FP64 ? sizeof(double) : sizeof(float));
+    if (prec == WSG_FP64) return (size_t)2 * T * (T + 2 * K + 1) * sizeof(double);
+    constexpr int AW = T + 4 * K;
+    constexpr int AP = AW | 1;
+    return ((size_t)(2 * AW * AP * 4) + 15) / 16 * 16 + (size_t)kStage * sizeof(uint4);
 }
 
 template <int T, int K> const void *grid_kernel(int prec)
@@ -292,14 +408,14 @@ int grid_max_ctas_per_sm(int prec, int tile, int half)
 }
 
 cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b, const RecBuffers &r,
-                        void *grid, int ctas, int chunk, cudaStream_t s)
+                        void *grid, void *partials, int ctas, cudaStream_t s)
 {
     size_t smem = 0;
     const void *k = grid_pick(prec, g.tile, g.half, smem);
     if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    GridArgs a{g, b, r, grid, chunk};
+    GridArgs a{g, b, r, grid, partials};
     void *args[] = {&a};
     return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
 }

@@ -12,7 +12,8 @@
 //
 // The array is a fixed 64 MiB of device memory per GPU that loads the library,
 // held until the process exits.  A call needs
-//     256 + 24*nbins + 160*num_points   bytes (plus 256-byte alignment padding),
+//     256 + 24*nbins + 8*ceil(nbins/4096) + 32768 + 160*num_points   bytes
+//     (plus 256-byte alignment padding),
 //     nbins = num_w_planes * ceil(grid_size_y/64) * ceil(grid_size_x/64),
 // and is rejected with WSG_ERR_CAPACITY when that exceeds the array: for a
 // 4096x4096x32 grid that is about 400,000 measurements per call.
@@ -149,14 +150,14 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     // scratch layout: counters | bin table | record cells | indices | fracs | values
     const unsigned long long cap = 4ull * (unsigned long long)(num_points > 0 ? num_points : 1);
     const size_t o_bins = up256(sizeof(DevCounters));
-    const size_t o_cell = o_bins + up256((size_t)6 * g.nbins * sizeof(unsigned));
+    const size_t o_cell = o_bins + up256(bin_buffer_bytes(g.nbins, max_split_items(cap, kDefaultSplit)));
     const size_t o_idx = o_cell + up256(cap * sizeof(unsigned));
     const size_t o_frac = o_idx + up256(cap * sizeof(unsigned));
     const size_t o_val = o_frac + up256(cap * sizeof(double2));
     const size_t need = o_val + up256(cap * sizeof(double2));
     if (g.nbins >= (1ll << 31) || need > kNoAllocBytes)
         return fail(WSG_ERR_CAPACITY,
-                    "wsg_grid_noalloc: needs %zu bytes of scratch (24*%lld bins + 160*%ld "
+                    "wsg_grid_noalloc: needs %zu bytes of scratch (about 24*%lld bins + 160*%ld "
                     "measurements), above its fixed %zu-byte array; pass fewer measurements "
                     "per call or use the plan API",
                     need, g.nbins, num_points, kNoAllocBytes);
@@ -170,13 +171,10 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     BinBuffers b;
     b.ctr = reinterpret_cast<DevCounters *>(s);
     unsigned *bins = reinterpret_cast<unsigned *>(s + o_bins);
-    b.cnt_prim = bins;
-    b.cnt_dup = bins + g.nbins;
-    b.cur_prim = bins + 2 * g.nbins;
-    b.cur_dup = bins + 3 * g.nbins;
-    b.off = bins + 4 * g.nbins;
-    b.order = bins + 5 * g.nbins;
+    bin_buffer_carve(bins, g.nbins, b);
+    b.split_size = kDefaultSplit;
     RecBuffers r;
+    r.rec16 = nullptr;
     r.cell = reinterpret_cast<unsigned *>(s + o_cell);
     r.idx = reinterpret_cast<unsigned *>(s + o_idx);
     r.frac = s + o_frac;
@@ -197,7 +195,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
         e = launch_bin_scatter(g, WSG_FP64, uu, vv, ww, vis_real, vis_img, weight, num_points,
                                freq_per_chan, polarizations, b, r, cs);
     if (e == cudaSuccess)
-        e = launch_grid(g, WSG_FP64, b, r, grid, per_sm * num_sms(), 0, cs);
+        e = launch_grid(g, WSG_FP64, b, r, grid, nullptr, per_sm * num_sms(), cs);
     if (e != cudaSuccess)
         return fail(WSG_ERR_CUDA, "wsg_grid_noalloc: %s", cudaGetErrorString(e));
     return WSG_OK;

@@ -30,6 +30,10 @@ constexpr double kRefPi = 3.14159265359;
 
 constexpr int kMaxHalf = 7;          // support up to 15 cells
 constexpr int kThreads = 256;        // threads per CTA for tile kernels
+constexpr int kScanThreads = 256;    // bin-size scan: threads per CTA
+constexpr int kScanPerBlock = 4096;  // bin-size scan: bins per CTA
+constexpr int kStage = 512;          // records staged in shared memory per pass
+constexpr int kDefaultSplit = 4096;  // records per work item of a split bin
 
 struct DevCounters {
     unsigned long long records;
@@ -39,7 +43,8 @@ struct DevCounters {
     unsigned int work_grid;
     unsigned int work_degrid;
     unsigned int error;
-    unsigned int pad[2];
+    unsigned int nsplit_items;   // work items of split bins (the list `split`)
+    unsigned int nslots;         // partial tiles needed by split bins
 };
 
 // Geometry of the coordinate step (w-stacking.cu:66-77) and the tiling.
@@ -51,18 +56,68 @@ struct GeomParams {
     long long nbins;
 };
 
+// Work decomposition.  A bin with more than `split` records is cut into
+// ceil(n/split) work items of at most `split` records; they are listed in
+// `split` (entry = bin | chunk << 32) and processed first.  Every other bin is
+// one work item.  Per bin (nbins u32 each): record counts (primary,
+// duplicate), scatter cursors, record offset, is-split flag, first partial
+// tile slot, finished-items counter.
 struct BinBuffers {
-    unsigned *cnt_prim, *cnt_dup, *cur_prim, *cur_dup, *off, *order;
+    unsigned *cnt_prim, *cnt_dup, *cur_prim, *cur_dup, *off, *is_split, *slot, *done;
+    unsigned long long *part;    // 2 * scan_blocks(nbins) entries (scan partials)
+    unsigned long long *split;   // split-item list
     DevCounters *ctr;
+    unsigned split_size;
 };
 
+// Records.  FP32C: rec16 (16 B, see k_bin_scatter) + idx.  FP64: cell, frac,
+// val (structure of arrays) + idx.
 struct RecBuffers {
+    uint4 *rec16;
     unsigned *cell;
-    void *frac;   // float2 or double2
-    void *val;    // float2 or double2
+    void *frac;   // double2
+    void *val;    // double2
     unsigned *idx;
     unsigned long long capacity;
 };
+
+// Bytes of BinBuffers storage for nbins bins and at most `items` split
+// items (u32 arrays, then the scan partials, then the split list; 256-byte
+// aligned).
+long long scan_blocks(long long nbins);
+inline size_t bin_buffer_bytes(long long nbins, unsigned long long items)
+{
+    const size_t a = ((size_t)8 * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
+    const size_t b = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
+    return a + b + (size_t)items * 8;
+}
+inline void bin_buffer_carve(void *base, long long nbins, BinBuffers &b)
+{
+    unsigned *u = reinterpret_cast<unsigned *>(base);
+    b.cnt_prim = u;
+    b.cnt_dup = u + nbins;
+    b.cur_prim = u + 2 * nbins;
+    b.cur_dup = u + 3 * nbins;
+    b.off = u + 4 * nbins;
+    b.is_split = u + 5 * nbins;
+    b.slot = u + 6 * nbins;
+    b.done = u + 7 * nbins;
+    unsigned char *c = reinterpret_cast<unsigned char *>(base);
+    const size_t a = ((size_t)8 * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
+    const size_t p = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
+    b.part = reinterpret_cast<unsigned long long *>(c + a);
+    b.split = reinterpret_cast<unsigned long long *>(c + a + p);
+}
+// Upper bounds for `records` records cut into items of `split`: split items
+// and partial-tile slots.
+inline unsigned long long max_split_items(unsigned long long records, unsigned split)
+{
+    return 2 * (records / split) + 1;
+}
+inline unsigned long long max_slots(unsigned long long records, unsigned split)
+{
+    return records / split + 1;
+}
 
 // Pixel-geometry table of the FP32C w-correction (per pixel, planar):
 // the phase in cycles for plane w is a + w*b (mod 1), a and b as
@@ -84,8 +139,10 @@ cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu,
                                cudaStream_t s);
 
 // ---- launchers (grid.cu) ----
+// partials: FP32C partial tiles of split bins (max_slots * tile^2 float2),
+// unused for FP64.
 cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b,
-                        const RecBuffers &r, void *grid, int ctas, int chunk,
+                        const RecBuffers &r, void *grid, void *partials, int ctas,
                         cudaStream_t s);
 int grid_max_ctas_per_sm(int prec, int tile, int half);
 

@@ -151,7 +151,7 @@ def test_plan_grid_fp64(medium, tile):
     assert st["dropped_plane"] == 0 and st["points_in"] == o.n
 
 
-@pytest.mark.parametrize("tile,chunk", [(64, 2048), (32, 64)])
+@pytest.mark.parametrize("tile,chunk", [(64, 4096), (32, 512)])
 def test_plan_grid_fp32c(medium, tile, chunk):
     import torch
     o = medium["obs"]
@@ -177,6 +177,32 @@ def test_plan_image_forward(medium, precision, tol):
     got = np.stack([z[..., 0][ok], z[..., 1][ok]])
     ref = np.stack([re[ok], im[ok]])
     assert _nrm_rms(got, ref) <= tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32c", 2e-6)])
+def test_concentrated_bins_are_split_and_combined(precision, tol):
+    """150k measurements inside a few cells: bins far above the split size are
+    cut into work items whose partial tiles are combined (FP32C), or gridded
+    whole (FP64); both must match the oracle."""
+    import torch
+    from lofar_gb300 import Plan
+    rng = np.random.default_rng(21)
+    n, nx, planes = 150_000, 128, 2
+    uu = 0.5 + rng.normal(0, 1.5 / nx, n)
+    vv = 0.37 + rng.normal(0, 1.5 / nx, n)
+    ww = rng.random(n) * 0.999
+    vr = rng.standard_normal(n).astype(np.float32)
+    vi = rng.standard_normal(n).astype(np.float32)
+    wt = np.ones(n, np.float32)
+    ref = O.wstack(uu, vv, ww, vr, vi, wt, num_w_planes=planes, dx=1 / nx, dw=1 / planes,
+                   w_support=7, nx=nx, ny=nx)
+    p = Plan(nx, nx, planes, 7, precision=precision)
+    p.set_tuning(chunk=512)
+    p.bin(uu, vv, ww, vr, vi, wt)
+    g = torch.view_as_real(p.grid()).double().cpu().numpy()
+    assert p.stats()["max_bin_records"] > 20 * 512
+    assert _nrm_rms(g, ref) <= tol
+    assert _nrm_max(g, ref) <= 10 * tol
 
 
 def test_single_measurement_indices_bit_exact():
