@@ -72,6 +72,8 @@ __device__ __forceinline__ unsigned bin_index(const GeomParams &g, int w, int tv
 // operations in flight per thread.
 constexpr int kItems = 4;
 
+__device__ __forceinline__ unsigned sub_of(long long m) { return (unsigned)(m >> 8) & (kSub - 1); }
+
 template <bool UP2, bool WP2>
 __global__ void __launch_bounds__(256)
 k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
@@ -79,6 +81,7 @@ k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restric
 {
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x * kItems;
+    const long long nb = g.nbins;
     for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
         double x[kItems], y[kItems], z[kItems];
 #pragma unroll
@@ -97,14 +100,17 @@ k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restric
             const int st = m < n ? measure<UP2, WP2, float>(g, x[i], y[i], z[i], o, fu, fv) : 3;
             ndp += st == 1;
             ndw += st == 2;
+            const unsigned sub = sub_of(m);
             const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
             const unsigned peers = __match_any_sync(kFull, prim);
             if (st == 0) {
-                if (lane == __ffs(peers) - 1) atomicAdd(&b.cnt_prim[prim], (unsigned)__popc(peers));
+                // lanes of one warp share m >> 8, hence the sub-counter
+                if (lane == __ffs(peers) - 1)
+                    atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
                 for (int tv = o.tv0; tv <= o.tv1; tv++)
                     for (int tu = o.tu0; tu <= o.tu1; tu++)
                         if (tv != o.tvp || tu != o.tup)
-                            atomicAdd(&b.cnt_dup[bin_index(g, o.gw, tv, tu)], 1u);
+                            atomicAdd(&b.sub_dup[sub * nb + bin_index(g, o.gw, tv, tu)], 1u);
             }
         }
         for (int d = 16; d >= 1; d >>= 1) {
@@ -164,6 +170,7 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     const long long stride = (long long)gridDim.x * blockDim.x * kItems;
+    const long long nb = g.nbins;
     for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
         double x[kItems], y[kItems], z[kItems];
 #pragma unroll
@@ -173,48 +180,46 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             y[i] = m < n ? __ldcs(vv + m) : 0.0;
             z[i] = m < n ? __ldcs(ww + m) : 0.0;
         }
-        MGeom o[kItems];
-        S fu[kItems], fv[kItems];
-        int st[kItems];
-        unsigned basep[kItems], peers[kItems];
+        // primary positions first (one aggregated cursor atomic per bin and warp)
+        unsigned ppos[kItems];
 #pragma unroll
         for (int i = 0; i < kItems; i++) {
             const long long m = base + (long long)i * blockDim.x + threadIdx.x;
-            fu[i] = fv[i] = 0;
-            st[i] = m < n ? measure<UP2, WP2, S>(g, x[i], y[i], z[i], o[i], fu[i], fv[i]) : 3;
-            const unsigned prim = (st[i] == 0) ? bin_index(g, o[i].gw, o[i].tvp, o[i].tup) : kFull;
-            peers[i] = __match_any_sync(kFull, prim);
-            const int leader = __ffs(peers[i]) - 1;
+            MGeom o;
+            S fu, fv;
+            const int st = m < n ? measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv) : 3;
+            const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
+            const unsigned peers = __match_any_sync(kFull, prim);
+            const int leader = __ffs(peers) - 1;
             unsigned got = 0;
-            if (st[i] == 0 && lane == leader)
-                got = atomicAdd(&b.cur_prim[prim], (unsigned)__popc(peers[i]));
-            basep[i] = __shfl_sync(kFull, got, leader);
+            if (st == 0 && lane == leader)
+                got = atomicAdd(&b.sub_prim[sub_of(m) * nb + prim], (unsigned)__popc(peers));
+            const unsigned basep = __shfl_sync(kFull, got, leader);
+            ppos[i] = (st == 0) ? basep + (unsigned)__popc(peers & lt_mask) : 0xFFFFFFFFu;
         }
 #pragma unroll
         for (int i = 0; i < kItems; i++) {
-            if (st[i] != 0) continue;
+            if (ppos[i] == 0xFFFFFFFFu) continue;
             const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+            MGeom o;
+            S fu, fv;
+            measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv);
             S re, im;
             fold_value<S>(vr, vi, wt, m, nf, np, re, im);
-            for (int tv = o[i].tv0; tv <= o[i].tv1; tv++) {
-                for (int tu = o[i].tu0; tu <= o[i].tu1; tu++) {
-                    const unsigned bin = bin_index(g, o[i].gw, tv, tu);
-                    unsigned pos;
-                    if (tv == o[i].tvp && tu == o[i].tup) {
-                        pos = b.off[bin] + basep[i] + (unsigned)__popc(peers[i] & lt_mask);
-                    } else {
-                        const unsigned tot = b.cnt_prim[bin] + b.cnt_dup[bin];
-                        pos = b.off[bin] + tot - 1u - atomicAdd(&b.cur_dup[bin], 1u);
-                    }
-                    const int cu = o[i].gu - tu * g.tile;
-                    const int cv = o[i].gv - tv * g.tile;
+            for (int tv = o.tv0; tv <= o.tv1; tv++) {
+                for (int tu = o.tu0; tu <= o.tu1; tu++) {
+                    const unsigned bin = bin_index(g, o.gw, tv, tu);
+                    const unsigned pos = (tv == o.tvp && tu == o.tup)
+                                             ? ppos[i]
+                                             : atomicAdd(&b.sub_dup[sub_of(m) * nb + bin], 1u);
+                    const int cu = o.gu - tu * g.tile;
+                    const int cv = o.gv - tv * g.tile;
                     if (PREC == WSG_FP64) {
                         r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
-                        reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu[i], fv[i]);
+                        reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu, fv);
                         reinterpret_cast<double2 *>(r.val)[pos] = make_double2(re, im);
                     } else {
-                        r.rec16[pos] = make_uint4(pack_axis(cu, (float)fu[i]),
-                                                  pack_axis(cv, (float)fv[i]),
+                        r.rec16[pos] = make_uint4(pack_axis(cu, (float)fu), pack_axis(cv, (float)fv),
                                                   __float_as_uint((float)re),
                                                   __float_as_uint((float)im));
                     }
@@ -246,7 +251,9 @@ __global__ void __launch_bounds__(kScanThreads) k_bin_scan_a(long long nbins, Bi
     for (int k = 0; k < kScanPerBlock / kScanThreads; k++) {
         const long long i = beg + (long long)k * kScanThreads + tid;
         if (i < nbins) {
-            const unsigned t = b.cnt_prim[i] + b.cnt_dup[i];
+            unsigned t = 0;
+#pragma unroll
+            for (int q = 0; q < kSub; q++) t += b.sub_prim[q * nbins + i] + b.sub_dup[q * nbins + i];
             const unsigned it = split_items(t, b.split_size);
             rec += t;
             pk += (unsigned long long)it | ((unsigned long long)(it ? it - 1 : 0) << 32);
@@ -341,10 +348,16 @@ __global__ void __launch_bounds__(kScanThreads) k_bin_scan_c(long long nbins, Bi
     const long long beg = (long long)blockIdx.x * kScanPerBlock;
     constexpr int PER = kScanPerBlock / kScanThreads;   // consecutive bins per thread
     unsigned long long l0 = 0, l1 = 0;
+    unsigned tt[PER];
 #pragma unroll
     for (int k = 0; k < PER; k++) {
         const long long i = beg + (long long)tid * PER + k;
-        const unsigned t = i < nbins ? b.cnt_prim[i] + b.cnt_dup[i] : 0u;
+        unsigned t = 0;
+        if (i < nbins) {
+#pragma unroll
+            for (int q = 0; q < kSub; q++) t += b.sub_prim[q * nbins + i] + b.sub_dup[q * nbins + i];
+        }
+        tt[k] = t;
         const unsigned it = split_items(t, b.split_size);
         l0 += t;
         l1 += (unsigned long long)it | ((unsigned long long)(it ? it - 1 : 0) << 32);
@@ -385,8 +398,22 @@ __global__ void __launch_bounds__(kScanThreads) k_bin_scan_c(long long nbins, Bi
     for (int k = 0; k < PER; k++) {
         const long long i = beg + (long long)tid * PER + k;
         if (i >= nbins) break;
-        const unsigned t = b.cnt_prim[i] + b.cnt_dup[i];
+        const unsigned t = tt[k];
         const unsigned it = split_items(t, b.split_size);
+        // sub-range starts: primaries of sub 0..kSub-1, then duplicates
+        unsigned run = (unsigned)r0;
+        for (int q = 0; q < kSub; q++) {
+            const unsigned c = b.sub_prim[q * nbins + i];
+            b.sub_prim[q * nbins + i] = run;
+            run += c;
+        }
+        b.nprim[i] = run - (unsigned)r0;
+        for (int q = 0; q < kSub; q++) {
+            const unsigned c = b.sub_dup[q * nbins + i];
+            b.sub_dup[q * nbins + i] = run;
+            run += c;
+        }
+        b.ntotal[i] = t;
         b.off[i] = (unsigned)r0;
         b.is_split[i] = it ? 1u : 0u;
         b.slot[i] = (unsigned)(r1 >> 32);

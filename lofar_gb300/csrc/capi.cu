@@ -462,7 +462,7 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
         return set_error(WSG_ERR_ARG, "NULL input pointer");
     WSG_TRY(ensure_records(p, n));
     const BinBuffers b = p->binbufs();
-    WSG_CUDA(cudaMemsetAsync(b.cnt_prim, 0, sizeof(unsigned) * 4 * p->geom.nbins, p->stream));
+    WSG_CUDA(cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(p->geom.nbins), p->stream));
     WSG_CUDA(cudaMemsetAsync(b.ctr, 0, sizeof(DevCounters), p->stream));
     WSG_CUDA(launch_bin_count(p->geom, uu, vv, ww, n, b, p->stream));
     WSG_CUDA(launch_bin_scan(p->geom, b, p->stream));

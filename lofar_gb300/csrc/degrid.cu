@@ -68,7 +68,7 @@ __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, 
         bin = item - nsplit;
         if (b.is_split[bin]) return false;
     }
-    const unsigned nprim = b.cnt_prim[bin];
+    const unsigned nprim = b.nprim[bin];
     if (item < nsplit) {
         p0 = min(nprim, chunk * b.split_size);
         p1 = min(nprim, p0 + b.split_size);
@@ -145,8 +145,8 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
                 const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float du = off1 - fu, dv = off1 - fv;
-                const float gu = norm * exp2f(du * du * c2);
-                const float gv = on ? exp2f(dv * dv * c2) : 0.0f;
+                const float gu = norm * fast_exp2(du * du * c2);
+                const float gv = on ? fast_exp2(dv * dv * c2) : 0.0f;
                 const int row = (cv - K + kk + H) * AP + (cu - K + H);
                 float sr = 0.f, si = 0.f;
 #pragma unroll

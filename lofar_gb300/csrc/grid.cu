@@ -46,6 +46,9 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
     lo += e;
 }
 
+constexpr float kRoundMagic = 12582912.0f;   // 1.5 * 2^23
+constexpr int kRoundMagicBits = 0x4B400000;    // its bit pattern
+
 __device__ __forceinline__ void decode_bin(const GeomParams &g, unsigned bin, int &w, int &u0,
                                            int &v0)
 {
@@ -111,6 +114,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
     __shared__ int s_last;
     constexpr int NB = (AW + 7) / 8;   // 8x8-cell blocks of the accumulator
     __shared__ float s_part[NW];
+    __shared__ float s_vmax[NW];
     __shared__ float s_blk[NB * NB];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -140,7 +144,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         decode_bin(a.g, bin, w, u0, v0);
         const int tx = min(T, a.g.nx - u0);
         const int ty = min(T, a.g.ny - v0);
-        const unsigned total = a.b.cnt_prim[bin] + a.b.cnt_dup[bin];
+        const unsigned total = a.b.ntotal[bin];
         const bool is_split = item < nsplit;
         const unsigned r0 = chunk * split;
         const unsigned r1 = is_split ? min(total, r0 + split) : total;
@@ -153,13 +157,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         // bounds every cell of the item.
         for (int i = tid; i < NB * NB; i += kThreads) s_blk[i] = 0.0f;
         __syncthreads();
+        float vmax = 0.0f;
         for (unsigned i = r0 + tid; i < r1; i += kThreads) {
             const uint4 q = __ldcg(rec + off + i);
             const int bx = ((int)(q.x >> 24) - 64 + H) >> 3;
             const int by = ((int)(q.y >> 24) - 64 + H) >> 3;
-            atomicAdd(&s_blk[by * NB + bx],
-                      fabsf(__uint_as_float(q.z)) + fabsf(__uint_as_float(q.w)));
+            const float ar = fabsf(__uint_as_float(q.z)), ai = fabsf(__uint_as_float(q.w));
+            vmax = fmaxf(vmax, fmaxf(ar, ai));
+            atomicAdd(&s_blk[by * NB + bx], ar + ai);
         }
+        for (int d = 16; d >= 1; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xFFFFFFFFu, vmax, d));
+        if (lane == 0) s_vmax[warp] = vmax;
         __syncthreads();
         float bmax = 0.0f;
         for (int i = tid; i < NB * NB; i += kThreads) {
@@ -173,16 +181,22 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         for (int d = 16; d >= 1; d >>= 1) bmax = fmaxf(bmax, __shfl_xor_sync(0xFFFFFFFFu, bmax, d));
         if (lane == 0) s_part[warp] = bmax;
         __syncthreads();
-        float bound = 0.0f;
+        float bound = 0.0f, tapmax = 0.0f;
 #pragma unroll
-        for (int i = 0; i < NW; i++) bound = fmaxf(bound, s_part[i]);
-        // cell sums stay below 2^30 (+ at most one rounding per term)
+        for (int i = 0; i < NW; i++) {
+            bound = fmaxf(bound, s_part[i]);
+            tapmax = fmaxf(tapmax, s_vmax[i]);
+        }
+        // cell sums stay below 2^30 (+ at most one rounding per term) and
+        // every scaled tap below 2^22 (exact rounding with one FMA, below)
         bound = bound * norm * 1.0001f;
+        tapmax = tapmax * norm * 1.0001f;
         int fexp = 30;
         if (bound > 0.0f) {
-            int e2;
-            frexpf(bound, &e2);   // bound < 2^e2
-            fexp = min(30 - e2, 100);
+            int e2, e3;
+            frexpf(bound, &e2);    // bound < 2^e2
+            frexpf(tapmax, &e3);   // tapmax < 2^e3
+            fexp = min(min(30 - e2, 22 - e3), 100);
         }
         const float scale = ldexpf(1.0f, fexp);
         const float inv = ldexpf(1.0f, -fexp);
@@ -201,8 +215,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
                 const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float du = off1 - fu, dv = off1 - fv;
-                const float gu = norm * exp2f(du * du * c2);
-                const float gv = exp2f(dv * dv * c2) * scale;
+                const float gu = norm * fast_exp2(du * du * c2);
+                const float gv = fast_exp2(dv * dv * c2) * scale;
                 const float ar = __uint_as_float(q.z) * gv;
                 const float ai = __uint_as_float(q.w) * gv;
                 const int row = (cv - K + k + H) * AP + (cu - K + H);
@@ -210,8 +224,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
                 for (int j = 0; j < NT; j++) {
                     const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
                     if (valid) {
-                        atomicAdd(are + row + j, __float2int_rn(ar * g));
-                        atomicAdd(aim + row + j, __float2int_rn(ai * g));
+                        // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds
+                        // it to an integer held in the low mantissa bits
+                        atomicAdd(are + row + j,
+                                  __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits);
+                        atomicAdd(aim + row + j,
+                                  __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits);
                     }
                 }
             }
@@ -312,7 +330,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         const int tx = min(T, a.g.nx - u0);
         const int ty = min(T, a.g.ny - v0);
         const unsigned off = a.b.off[bin];
-        const unsigned n = a.b.cnt_prim[bin] + a.b.cnt_dup[bin];
+        const unsigned n = a.b.ntotal[bin];
 
         for (unsigned rr = warp; rr < n; rr += NW) {
             const unsigned cell = __ldg(a.r.cell + off + rr);

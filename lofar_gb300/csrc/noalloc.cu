@@ -188,7 +188,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
 
     // the array keeps the previous call's contents: clear counters and bin counts
     cudaError_t e = cudaMemsetAsync(b.ctr, 0, sizeof(DevCounters), cs);
-    if (e == cudaSuccess) e = cudaMemsetAsync(bins, 0, (size_t)4 * g.nbins * sizeof(unsigned), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(g.nbins), cs);
     if (e == cudaSuccess) e = launch_bin_count(g, uu, vv, ww, num_points, b, cs);
     if (e == cudaSuccess) e = launch_bin_scan(g, b, cs);
     if (e == cudaSuccess)

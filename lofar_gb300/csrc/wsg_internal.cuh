@@ -59,13 +59,19 @@ struct GeomParams {
 // Work decomposition.  A bin with more than `split` records is cut into
 // ceil(n/split) work items of at most `split` records; they are listed in
 // `split` (entry = bin | chunk << 32) and processed first.  Every other bin is
-// one work item.  Per bin (nbins u32 each): record counts (primary,
-// duplicate), scatter cursors, record offset, is-split flag, first partial
-// tile slot, finished-items counter.
+// one work item.
+//
+// Counting uses kSub sub-counters per bin (measurement m uses sub-counter
+// (m >> 8) % kSub in both passes), which spreads the atomics of crowded bins
+// over kSub addresses.  After the scan, sub_prim[s][b] / sub_dup[s][b] hold
+// the first record position of sub-range s of bin b's primaries / duplicates
+// and the scatter advances them as cursors.
+constexpr int kSub = 8;
 struct BinBuffers {
-    unsigned *cnt_prim, *cnt_dup, *cur_prim, *cur_dup, *off, *is_split, *slot, *done;
-    unsigned long long *part;    // 2 * scan_blocks(nbins) entries (scan partials)
-    unsigned long long *split;   // split-item list
+    unsigned *sub_prim, *sub_dup;            // [kSub][nbins]
+    unsigned *off, *nprim, *ntotal, *is_split, *slot, *done;   // [nbins]
+    unsigned long long *part;                // 2 * scan_blocks(nbins) entries
+    unsigned long long *split;               // split-item list
     DevCounters *ctr;
     unsigned split_size;
 };
@@ -85,29 +91,33 @@ struct RecBuffers {
 // items (u32 arrays, then the scan partials, then the split list; 256-byte
 // aligned).
 long long scan_blocks(long long nbins);
+constexpr int kBinU32PerBin = 2 * kSub + 6;
 inline size_t bin_buffer_bytes(long long nbins, unsigned long long items)
 {
-    const size_t a = ((size_t)8 * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
+    const size_t a = ((size_t)kBinU32PerBin * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
     const size_t b = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
     return a + b + (size_t)items * 8;
 }
 inline void bin_buffer_carve(void *base, long long nbins, BinBuffers &b)
 {
     unsigned *u = reinterpret_cast<unsigned *>(base);
-    b.cnt_prim = u;
-    b.cnt_dup = u + nbins;
-    b.cur_prim = u + 2 * nbins;
-    b.cur_dup = u + 3 * nbins;
-    b.off = u + 4 * nbins;
-    b.is_split = u + 5 * nbins;
-    b.slot = u + 6 * nbins;
-    b.done = u + 7 * nbins;
+    b.sub_prim = u;
+    b.sub_dup = u + kSub * nbins;
+    unsigned *v = u + 2 * kSub * nbins;
+    b.off = v;
+    b.nprim = v + nbins;
+    b.ntotal = v + 2 * nbins;
+    b.is_split = v + 3 * nbins;
+    b.slot = v + 4 * nbins;
+    b.done = v + 5 * nbins;
     unsigned char *c = reinterpret_cast<unsigned char *>(base);
-    const size_t a = ((size_t)8 * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
+    const size_t a = ((size_t)kBinU32PerBin * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
     const size_t p = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
     b.part = reinterpret_cast<unsigned long long *>(c + a);
     b.split = reinterpret_cast<unsigned long long *>(c + a + p);
 }
+// Bytes of the sub-counters (cleared before each binning).
+inline size_t bin_counter_bytes(long long nbins) { return (size_t)2 * kSub * nbins * sizeof(unsigned); }
 // Upper bounds for `records` records cut into items of `split`: split items
 // and partial-tile slots.
 inline unsigned long long max_split_items(unsigned long long records, unsigned split)
@@ -177,5 +187,14 @@ cudaError_t launch_f32_to_f64(const float2 *in, double2 *out, long long n, cudaS
 
 int num_sms();
 int report_status(int status, const char *msg);
+
+// 2^x from the hardware approximation (PTX ex2.approx: relative error about
+// 2^-22); used for the FP32C kernel weights, with x <= 0.
+__device__ __forceinline__ float fast_exp2(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 }  // namespace wsg
