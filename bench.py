@@ -84,14 +84,16 @@ def workload(args, backend):
 
 
 def algorithmic_bytes(n, nx, ny, planes, sc):
-    """Per-stage algorithmic bytes (read inputs once, write outputs once)."""
+    """Per-stage algorithmic bytes (read inputs once, write outputs once).
+
+    The FFT + w-correction stages count one read of the grid and one write of
+    the image (and the reverse for the adjoint): the transformed planes are
+    an intermediate of the fused kernels."""
     cells = planes * nx * ny
     return {
         "grid": n * (24 + 8 + 4) + cells * sc,          # bin + grid: inputs in, grid out
-        "fft_fwd": 2 * cells * sc,
-        "wcorrect": cells * sc + nx * ny * sc,
-        "wcorrect_adj": nx * ny * sc + cells * sc,
-        "fft_adj": 2 * cells * sc,
+        "fft_wcorrect": cells * sc + nx * ny * sc,
+        "wcorrect_adj_fft": nx * ny * sc + cells * sc,
         "degrid": cells * sc + n * 24 + n * sc,          # grid + uvw in, values out
     }
 
@@ -156,9 +158,11 @@ class ClockSampler:
 # our implementation
 # ---------------------------------------------------------------------------
 
-STAGES = ["bin", "grid", "fft_fwd", "wcorrect", "wcorrect_adj", "fft_adj", "degrid"]
-OUR_KERNELS_PER_STEP = {"bin": 5, "grid": 1, "fft_fwd": 0, "wcorrect": 1, "wcorrect_adj": 1,
-                        "fft_adj": 0, "degrid": 1}
+STAGES = ["bin", "grid", "fft_wcorrect", "wcorrect_adj_fft", "degrid"]
+# count + scan(3) + scatter + tile masks; grid; column FFT + row FFT/w-correction;
+# row FFT/adjoint w-correction + column FFT; degrid
+OUR_KERNELS_PER_STEP = {"bin": 6, "grid": 1, "fft_wcorrect": 2, "wcorrect_adj_fft": 2,
+                        "degrid": 1}
 
 
 def run_plan_steps(plan, ins, image, out, steps, record_stages):
@@ -181,21 +185,15 @@ def run_plan_steps(plan, ins, image, out, steps, record_stages):
         grid = plan.grid(plan_grid(plan))
         if evs:
             evs[2].record(stream)
-        plan.fft(grid, +1)
+        plan.fft_wcorrect(grid, out=image)
         if evs:
             evs[3].record(stream)
-        plan.wcorrect(grid, 1.0 / npix, out=image)
+        plan.wcorrect_adjoint_fft(image, out=grid)
         if evs:
             evs[4].record(stream)
-        plan.wcorrect_adjoint(image, 1.0 / npix, out=grid)
-        if evs:
-            evs[5].record(stream)
-        plan.fft(grid, -1)
-        if evs:
-            evs[6].record(stream)
         plan.degrid(grid, out=out)
         if evs:
-            evs[7].record(stream)
+            evs[5].record(stream)
             pending.append(evs)
     stop.record(stream)
     torch.cuda.synchronize()
@@ -443,7 +441,7 @@ def roofline(per, n, nx, P, sc, peak, peak_kind):
     grid_ms = med["bin"] + med["grid"]
     stages["gridding(bin+grid)"] = dict(ms=grid_ms, bytes=ab["grid"],
                                         gbs=ab["grid"] / (grid_ms * 1e-3) / 1e9)
-    for s in ("fft_fwd", "wcorrect", "wcorrect_adj", "fft_adj", "degrid"):
+    for s in ("fft_wcorrect", "wcorrect_adj_fft", "degrid"):
         stages[s] = dict(ms=med[s], bytes=ab[s], gbs=ab[s] / (med[s] * 1e-3) / 1e9)
     for v in stages.values():
         v["frac"] = v["gbs"] / peak

@@ -172,6 +172,18 @@ WSG_API int wsg_wcorrect_adjoint(wsg_plan *plan, const void *image, void *planes
  * plan precision), [num_points] complex, overwritten. */
 WSG_API int wsg_degrid(wsg_plan *plan, const void *grid, void *out);
 
+/* Per-plane inverse FFT (exponent +i) of `grid` followed by the w-correction
+ * into `image` (scale 1/(Nx*Ny) included); `grid` is overwritten.  With
+ * prune = 1 the grid must be the one gridded from the last wsg_bin: tiles
+ * without measurements are taken as zero and never read, and for FP32C
+ * power-of-two grids the two steps run fused (the transformed planes never
+ * reach memory).  prune = 0 transforms every cell. */
+WSG_API int wsg_fft_wcorrect(wsg_plan *plan, void *grid, void *image, int prune);
+/* Adjoint of wsg_fft_wcorrect: w-correction adjoint, then per-plane FFT
+ * (exponent -i), into `grid`.  With prune = 1 only the cells that wsg_degrid
+ * reads for the last wsg_bin are guaranteed to be written. */
+WSG_API int wsg_wcorrect_adjoint_fft(wsg_plan *plan, const void *image, void *grid, int prune);
+
 /* Forward imaging: bin + grid + FFT + w-correction into image
  * ([Ny][Nx] complex, plan precision).  Uses the plan's resident grid. */
 WSG_API int wsg_image_forward(wsg_plan *plan, long num_points, long freq_per_chan, long polarizations,

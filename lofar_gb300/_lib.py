@@ -73,6 +73,8 @@ SIGNATURES = {
     "wsg_wcorrect": (_I, [_P, _P, _P, _D]),
     "wsg_wcorrect_adjoint": (_I, [_P, _P, _P, _D]),
     "wsg_degrid": (_I, [_P, _P, _P]),
+    "wsg_fft_wcorrect": (_I, [_P, _P, _P, _I]),
+    "wsg_wcorrect_adjoint_fft": (_I, [_P, _P, _P, _I]),
     "wsg_image_forward": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
     "wsg_image_adjoint": (_I, [_P, _P, _P]),
     "wsg_image_forward_host": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),

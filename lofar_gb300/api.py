@@ -206,6 +206,22 @@ class Plan:
                                             float(scale)))
         return out
 
+    def fft_wcorrect(self, grid, out=None, prune=True):
+        """Inverse per-plane FFT of `grid` (overwritten) + w-correction -> image."""
+        out = self._torch.empty((self.ny, self.nx), dtype=self.cdtype, device="cuda") if out is None else out
+        self._sync_stream()
+        check(self.lib.wsg_fft_wcorrect(self._h, grid.data_ptr(), out.data_ptr(), int(bool(prune))))
+        return out
+
+    def wcorrect_adjoint_fft(self, image, out=None, prune=True):
+        """Adjoint of fft_wcorrect -> grid (with prune, only the degridded cells)."""
+        out = self.new_grid() if out is None else out
+        image = image.to(self.cdtype).contiguous()
+        self._sync_stream()
+        check(self.lib.wsg_wcorrect_adjoint_fft(self._h, image.data_ptr(), out.data_ptr(),
+                                                int(bool(prune))))
+        return out
+
     def degrid(self, grid, out=None):
         if self.n_binned is None:
             raise WstackError(_lib.WSG_ERR_STATE, "degrid before bin")

@@ -5,6 +5,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -164,6 +165,12 @@ struct wsg_plan {
     int fft_batch = 0;
     DevBuf fft_work;
 
+    // FP32C fused FFT + w-correction (power-of-two grids)
+    bool fused = false;
+    bool tw_ready = false;
+    bool masks_valid = false;
+    DevBuf twx, twy, masks;
+
     size_t elem() const { return prec == WSG_FP64 ? sizeof(double2) : sizeof(float2); }
     long long npix() const { return (long long)nx * ny; }
     BinBuffers binbufs() const
@@ -230,6 +237,10 @@ int plan_configure(wsg_plan *p)
     if (og <= 0 || od <= 0)
         return set_error(WSG_ERR_UNSUPPORTED, "no tile kernel for tile=%d support=%d", p->tile,
                          p->support);
+    const char *fft_env = getenv("WSTACK_GB300_FFT");
+    p->fused = p->prec == WSG_FP32C && fft_fused_supported(p->nx, p->ny, p->tile) &&
+               !(fft_env && strcmp(fft_env, "cufft") == 0);
+    p->masks_valid = false;
     p->ctas_grid = p->ctas_user > 0 ? p->ctas_user : og * sms;
     p->ctas_degrid = p->ctas_user > 0 ? p->ctas_user : od * sms;
     p->rec_cap = 0;  // bin table and partial-tile sizes depend on tile and split
@@ -286,6 +297,36 @@ int ensure_fft(wsg_plan *p)
     WSG_CUFFT(cufftSetWorkArea(p->fft, p->fft_work.p));
     p->fft_batch = batch;
     p->fft_ready = true;
+    return WSG_OK;
+}
+
+FftMasks mask_view(const wsg_plan *p)
+{
+    FftMasks m;
+    const size_t nt = (size_t)p->planes * p->geom.ntv * p->geom.ntu;
+    const size_t nc = (size_t)p->planes * p->geom.ntu;
+    unsigned char *b = p->masks.as<unsigned char>();
+    m.occ_tile = b;
+    m.need_tile = b + nt;
+    m.occ_col = b + 2 * nt;
+    m.need_col = b + 2 * nt + nc;
+    m.plane_occ = b + 2 * nt + 2 * nc;
+    m.plane_need = b + 2 * nt + 2 * nc + p->planes;
+    return m;
+}
+
+int ensure_fused(wsg_plan *p)
+{
+    if (!p->tw_ready) {
+        WSG_CUDA(p->twx.ensure(sizeof(float2) * p->nx));
+        WSG_CUDA(p->twy.ensure(sizeof(float2) * p->ny));
+        WSG_CUDA(launch_twiddles(p->twx.as<float2>(), p->nx, p->stream));
+        WSG_CUDA(launch_twiddles(p->twy.as<float2>(), p->ny, p->stream));
+        p->tw_ready = true;
+    }
+    const size_t nt = (size_t)p->planes * p->geom.ntv * p->geom.ntu;
+    const size_t nc = (size_t)p->planes * p->geom.ntu;
+    WSG_CUDA(p->masks.ensure(2 * nt + 2 * nc + 2 * (size_t)p->planes));
     return WSG_OK;
 }
 
@@ -358,6 +399,9 @@ int wsg_plan_destroy(wsg_plan *p)
                       &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi, &p->h_wt, &p->h_image,
                       &p->h_out, &p->sinx, &p->siny, &p->wscreen, &p->fft_work};
     for (DevBuf *b : bufs) b->release();
+    p->twx.release();
+    p->twy.release();
+    p->masks.release();
     delete p;
     return WSG_OK;
 }
@@ -469,6 +513,12 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
     WSG_CUDA(launch_bin_scatter(p->geom, p->prec, uu, vv, ww, vr, vi, wt, n, nf, np, b,
                                 p->recbufs(), p->stream));
     p->n_binned = n;
+    p->masks_valid = false;
+    if (p->fused) {
+        WSG_TRY(ensure_fused(p));
+        WSG_CUDA(launch_fft_masks(p->geom, b, mask_view(p), p->stream));
+        p->masks_valid = true;
+    }
     return WSG_OK;
 }
 
@@ -489,6 +539,12 @@ int wsg_fft(wsg_plan *p, void *grid, int sign)
     clear_error();
     if (!p || !grid) return set_error(WSG_ERR_ARG, "NULL argument");
     if (sign != 1 && sign != -1) return set_error(WSG_ERR_ARG, "sign must be +1 or -1");
+    if (p->fused) {
+        WSG_TRY(ensure_fused(p));
+        WSG_CUDA(launch_fft2d_plain(p->geom, reinterpret_cast<float2 *>(grid), p->twx.as<float2>(),
+                                    p->twy.as<float2>(), sign, p->stream));
+        return WSG_OK;
+    }
     WSG_TRY(ensure_fft(p));
     WSG_CUFFT(cufftSetStream(p->fft, p->stream));
     const int dir = sign > 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
@@ -553,6 +609,53 @@ int wsg_degrid(wsg_plan *p, const void *grid, void *out)
     return WSG_OK;
 }
 
+int wsg_fft_wcorrect(wsg_plan *p, void *grid, void *image, int prune)
+{
+    clear_error();
+    if (!p || !grid || !image) return set_error(WSG_ERR_ARG, "NULL argument");
+    WSG_TRY(ensure_wscreen(p));
+    const double scale = 1.0 / (double)p->npix();
+    if (!p->fused) {
+        WSG_TRY(wsg_fft(p, grid, +1));
+        WSG_TRY(wsg_wcorrect(p, grid, image, scale));
+        return WSG_OK;
+    }
+    WSG_TRY(ensure_fused(p));
+    if (prune && !p->masks_valid) return set_error(WSG_ERR_STATE, "pruned transform before wsg_bin");
+    if (!prune) {
+        // dense transform: plain 2D FFT then the w-correction kernel
+        WSG_CUDA(launch_fft2d_plain(p->geom, reinterpret_cast<float2 *>(grid),
+                                    p->twx.as<float2>(), p->twy.as<float2>(), +1, p->stream));
+        WSG_TRY(wsg_wcorrect(p, grid, image, scale));
+        return WSG_OK;
+    }
+    WSG_CUDA(launch_image_fwd_fused(p->geom, reinterpret_cast<float2 *>(grid),
+                                    reinterpret_cast<float2 *>(image), p->twx.as<float2>(),
+                                    p->twy.as<float2>(), wsg_plan_wscreen(p), mask_view(p),
+                                    p->wc.phase_on && p->planes > 1, scale, p->stream));
+    return WSG_OK;
+}
+
+int wsg_wcorrect_adjoint_fft(wsg_plan *p, const void *image, void *grid, int prune)
+{
+    clear_error();
+    if (!p || !grid || !image) return set_error(WSG_ERR_ARG, "NULL argument");
+    WSG_TRY(ensure_wscreen(p));
+    const double scale = 1.0 / (double)p->npix();
+    if (!p->fused || !prune) {
+        WSG_TRY(wsg_wcorrect_adjoint(p, image, grid, scale));
+        WSG_TRY(wsg_fft(p, grid, -1));
+        return WSG_OK;
+    }
+    WSG_TRY(ensure_fused(p));
+    if (!p->masks_valid) return set_error(WSG_ERR_STATE, "pruned transform before wsg_bin");
+    WSG_CUDA(launch_image_adj_fused(p->geom, reinterpret_cast<const float2 *>(image),
+                                    reinterpret_cast<float2 *>(grid), p->twx.as<float2>(),
+                                    p->twy.as<float2>(), wsg_plan_wscreen(p), mask_view(p),
+                                    p->wc.phase_on && p->planes > 1, scale, p->stream));
+    return WSG_OK;
+}
+
 int wsg_image_forward(wsg_plan *p, long n, long nf, long np, const double *uu, const double *vv,
                       const double *ww, const float *vr, const float *vi, const float *wt,
                       void *image)
@@ -563,8 +666,7 @@ int wsg_image_forward(wsg_plan *p, long n, long nf, long np, const double *uu, c
     WSG_TRY(ensure_wscreen(p));
     WSG_TRY(wsg_bin(p, n, nf, np, uu, vv, ww, vr, vi, wt));
     WSG_TRY(wsg_grid(p, p->grid.p));
-    WSG_TRY(wsg_fft(p, p->grid.p, +1));
-    WSG_TRY(wsg_wcorrect(p, p->grid.p, image, 1.0 / (double)p->npix()));
+    WSG_TRY(wsg_fft_wcorrect(p, p->grid.p, image, 1));
     return WSG_OK;
 }
 
@@ -574,8 +676,7 @@ int wsg_image_adjoint(wsg_plan *p, const void *image, void *out)
     if (!p || !image) return set_error(WSG_ERR_ARG, "NULL argument");
     if (p->n_binned < 0) return set_error(WSG_ERR_STATE, "adjoint before a forward/bin call");
     WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->planes * p->npix()));
-    WSG_TRY(wsg_wcorrect_adjoint(p, image, p->grid.p, 1.0 / (double)p->npix()));
-    WSG_TRY(wsg_fft(p, p->grid.p, -1));
+    WSG_TRY(wsg_wcorrect_adjoint_fft(p, image, p->grid.p, 1));
     WSG_TRY(wsg_degrid(p, p->grid.p, out));
     return WSG_OK;
 }

@@ -182,6 +182,29 @@ cudaError_t launch_wcorrect_adj_f64(const WcParams &p, const double *sinx, const
                                     const double2 *image, double2 *planes, double scale,
                                     cudaStream_t s);
 cudaError_t launch_scale_f64(double2 *x, long long n, double scale, cudaStream_t s);
+
+// ---- launchers (fft.cu): FP32C per-plane FFTs fused with the w-correction ----
+// Tile masks derived from the bin table (u8 arrays).
+struct FftMasks {
+    unsigned char *occ_tile;    // [P][ntv][ntu] tile holds a measurement (forward input)
+    unsigned char *occ_col;     // [P][ntu]      tile column holds one
+    unsigned char *plane_occ;   // [P]
+    unsigned char *need_tile;   // [P][ntv][ntu] tile read by the degridder (3x3 dilation)
+    unsigned char *need_col;    // [P][ntu]
+    unsigned char *plane_need;  // [P]
+};
+bool fft_fused_supported(int nx, int ny, int tile);
+cudaError_t launch_twiddles(float2 *tw, int n, cudaStream_t s);
+cudaError_t launch_fft_masks(const GeomParams &g, const BinBuffers &b, const FftMasks &m,
+                             cudaStream_t s);
+cudaError_t launch_image_fwd_fused(const GeomParams &g, float2 *grid, float2 *image,
+                                   const float2 *twx, const float2 *twy, const WScreen &ws,
+                                   const FftMasks &m, bool phase, double scale, cudaStream_t s);
+cudaError_t launch_image_adj_fused(const GeomParams &g, const float2 *image, float2 *grid,
+                                   const float2 *twx, const float2 *twy, const WScreen &ws,
+                                   const FftMasks &m, bool phase, double scale, cudaStream_t s);
+cudaError_t launch_fft2d_plain(const GeomParams &g, float2 *grid, const float2 *twx,
+                               const float2 *twy, int sign, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double2 *in, float2 *out, long long n, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float2 *in, double2 *out, long long n, cudaStream_t s);
 
