@@ -16,6 +16,13 @@ and the reference's OpenMP CPU path (the oracle port) timed on a bounded
 sample on this host's cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --workload c4     # the (channel, polarisation) batch: 16 channels
+                                      # x 4 polarisations, 2048^2 x 16 planes each
+
+Roofline traffic (DRAM bytes per launch of the gridding stage's kernels) is
+read from the committed ncu launch-list summary of the same workload
+(profiles/launches_fwd_adj_4096x32_50M.md) and scaled by the records binned
+when the workload differs.
 """
 from __future__ import annotations
 
@@ -41,9 +48,14 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
+                    help="c2: one 4096^2 x 32 image (default); c4: the channel x pol batch")
+    ap.add_argument("--per-channel", type=int, default=8_000_000,
+                    help="c4: measurements per channel before flagging")
+    ap.add_argument("--channels", type=int, default=16)
     ap.add_argument("--nvis", type=int, default=50_000_000)
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--planes", type=int, default=32)
@@ -67,6 +79,29 @@ def peaks():
         except Exception:
             pass
     return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# ranks: replicas only (every rank runs the whole workload on its own GPU;
+# the path has no exchange step at one image per rank)
+# ---------------------------------------------------------------------------
+
+def max_over_ranks(x: float, world: int) -> float:
+    """The slowest rank's time (the job ends when the last rank does)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def whole_job_mvis(n_per_rank: int, world: int, ms_per_step: float) -> float:
+    """Visibilities of all ranks per second of the slowest rank, in millions."""
+    return n_per_rank * world / (ms_per_step * 1e-3) / 1e6
 
 
 # ---------------------------------------------------------------------------
@@ -96,6 +131,34 @@ def algorithmic_bytes(n, nx, ny, planes, sc):
         "wcorrect_adj_fft": nx * ny * sc + cells * sc,
         "degrid": cells * sc + n * 24 + n * sc,          # grid + uvw in, values out
     }
+
+
+PROFILE_MD = os.path.join(ROOT, "profiles", "launches_fwd_adj_4096x32_50M.md")
+GRIDDING_KERNELS = ("k_bin_count", "k_bin_scan_a", "k_bin_scan_b", "k_bin_scan_c",
+                    "k_bin_scatter", "k_fft_masks", "k_grid_f32c")
+PROFILE_RECORDS = 59_834_420   # records binned in the profiled run (4096^2 x 32, 50M)
+
+
+def profiled_traffic(records):
+    """DRAM bytes (read + write) per launch of the gridding-stage kernels, from
+    the ncu launch list, scaled to `records` records; None if unavailable."""
+    if not os.path.exists(PROFILE_MD):
+        return None
+    tot, seen = 0.0, set()
+    for ln in open(PROFILE_MD):
+        f = [x.strip().strip("`") for x in ln.split("|")]
+        if len(f) < 8 or not f[1].startswith("k_"):
+            continue
+        name = f[1].split("<")[0]
+        if name in GRIDDING_KERNELS:
+            try:
+                tot += (float(f[6]) + float(f[7])) * 1e9
+                seen.add(name)
+            except ValueError:
+                pass
+    if "k_grid_f32c" not in seen or "k_bin_scatter" not in seen:
+        return None
+    return tot * records / PROFILE_RECORDS
 
 
 # ---------------------------------------------------------------------------
@@ -247,14 +310,9 @@ def bench_ours(args, rank, world):
     clocks.start()
     total_ms, per = run_plan_steps(plan, ins, image, out, args.steps, True)
     clk = clocks.stop()
-    if world > 1:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-        dist.barrier()
+    total_ms = max_over_ranks(total_ms, world)
     ms_per_step = total_ms / args.steps
-    n_vis_total = n * world
-    value = n_vis_total / (ms_per_step * 1e-3) / 1e6
+    value = whole_job_mvis(n, world, ms_per_step)
 
     # forward image of the FP32C form (for the accuracy comparison)
     img32 = plan.image_forward(*ins).clone()
@@ -434,6 +492,156 @@ def bench_reference(args, rank, world):
     }
 
 
+# ---------------------------------------------------------------------------
+# the (channel, polarisation) batch
+# ---------------------------------------------------------------------------
+
+def batch_workload(args, backend):
+    from lofar_gb300 import synth
+    gen = dict(synth.CONFIGS["c4"]["gen"])
+    gen["n_per_channel"] = args.per_channel
+    gen["n_channels"] = args.channels
+    t = time.time()
+    obs = synth.observe_batch(backend=backend, **gen)
+    return obs, time.time() - t
+
+
+def bench_batch(args, rank, world, peak, peak_kind):
+    """All channel x pol jobs in one persistent gridding launch, the forward
+    replayed as one CUDA graph, tuning picked by the autotuner; beside it the
+    same jobs run one after another through the single-image plan."""
+    import torch
+    import torch.distributed as dist
+    from lofar_gb300 import Batch, Plan, synth
+
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    cfg = synth.CONFIGS["c4"]
+    nx, P, S = cfg["nx"], cfg["planes"], cfg["support"]
+    obs, gen_s = batch_workload(args, "torch")
+    C, pols = len(obs.channels), obs.pols
+    B = Batch(nx, nx, P, S, channels=C, pols=pols)
+    B.set_wcorrection(obs.resolution, obs.wmin, obs.wmax)
+    B.bind(obs.channels)
+    nvis = B.n_vis()
+    images = B.new_images()
+    out = torch.empty(nvis, dtype=torch.complex64, device="cuda")
+    best, tried = B.autotune(images, iters=2)
+    for _ in range(max(args.warmup, 1)):
+        B.forward(images, graph=True)
+        B.adjoint(images, out)
+    stats = B.stats()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    evs = []
+    clocks = ClockSampler(dev)
+    clocks.start()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        B.forward(images, graph=True)
+        e[1].record(stream)
+        B.adjoint(images, out)
+        e[2].record(stream)
+        evs.append(e)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = max_over_ranks(start.elapsed_time(stop), world)
+    ms = total_ms / args.steps
+    fwd = statistics.median(e[0].elapsed_time(e[1]) for e in evs)
+    adj = statistics.median(e[1].elapsed_time(e[2]) for e in evs)
+    if rank != 0:
+        return None
+
+    # end to end: pinned host inputs -> bound device buffers, forward + adjoint,
+    # images and model visibilities back to pinned host memory
+    host_in = [[torch.as_tensor(x).pin_memory() for x in ch] for ch in obs.channels]
+    himg = torch.empty(images.shape, dtype=torch.complex64).pin_memory()
+    hout = torch.empty(nvis, dtype=torch.complex64).pin_memory()
+
+    def e2e_step():
+        for dst, src in zip(B._bound, host_in):
+            for d, h in zip(dst, src):
+                d.copy_(h, non_blocking=True)
+        B.forward(images, graph=True)
+        B.adjoint(images, out)
+        himg.copy_(images, non_blocking=True)
+        hout.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    t0 = time.perf_counter()
+    n_e2e = max(args.e2e_steps, 1)
+    for _ in range(n_e2e):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / n_e2e
+    h2d = sum(int(h.numel() * h.element_size()) for ch in host_in for h in ch)
+    d2h = int(himg.numel() * 8 + hout.numel() * 8)
+
+    # the same jobs one after another through the single-image plan
+    pl = Plan(nx, nx, P, S, precision="fp32c")
+    pl.set_wcorrection(obs.resolution, obs.wmin, obs.wmax)
+    jobs = []
+    for c, ch in enumerate(B._bound):
+        for p in range(pols):
+            if ch[0].numel():
+                jobs.append((c, p, (ch[0], ch[1], ch[2], ch[3][p::pols].contiguous(),
+                                    ch[4][p::pols].contiguous(), ch[5][p::pols].contiguous())))
+    img1 = torch.empty((nx, nx), dtype=torch.complex64, device="cuda")
+    pl.reserve(max(j[2][0].numel() for j in jobs))
+
+    def seq_step():
+        for c, p, ins in jobs:
+            pl.image_forward(*ins, out=img1)
+            pl.image_adjoint(img1)
+
+    seq_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq_step()
+    torch.cuda.synchronize()
+    seq_ms = (time.perf_counter() - t0) * 1e3
+    pl.close()
+
+    cells = C * pols * P * nx * nx
+    ab = algorithmic_bytes(nvis, nx, nx, C * pols * P, 8)
+    # per job the image is nx*nx: the cube-wide formula counts one image, add the rest
+    ab_step = sum(ab.values()) + 2 * (C * pols - 1) * nx * nx * 8
+    gbs = ab_step / (ms * 1e-3) / 1e9
+    return {
+        "metric": METRIC, "value": whole_job_mvis(nvis, world, ms), "unit": "Mvis/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32c",
+        "data": "synthetic (seeded; 62 stations, 8 km, 8 h; channels uniform in 120-180 MHz, "
+                "per-channel flagging U(0, 60%), 4 polarisations of a weakly polarised sky)",
+        "config": {"workload": f"channel x pol batch: {C} channels x {pols} pols, one "
+                               f"{nx}x{nx} grid of {P} w-planes each, support {S}, "
+                               f"{nvis} visibilities ({args.per_channel} per channel before "
+                               f"flagging)",
+                   "graph": "forward replayed as one CUDA graph", "tuning": best,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
+        "forward_ms": fwd, "adjoint_ms": adj,
+        "roofline": {"bound": "hbm", "kernel": "whole step (bin, grid, FFT + w-correction, "
+                                                "adjoint, degrid)",
+                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                     "peak_source": f"{peak_kind} hbm copy bandwidth", "traffic": None,
+                     "algorithmic_bytes_per_launch": ab_step},
+        "sequential_single_image": {"ms_per_step": seq_ms, "jobs": len(jobs),
+                                    "batch_speedup": seq_ms / ms},
+        "autotune": {"best": best, "tried": tried},
+        "gpu_launches": args.steps * 12,   # 9 forward kernels (graph) + 3 adjoint
+        "clocks": clk, "binning": stats, "device_bytes": B.device_bytes(), "gen_s": gen_s,
+        "e2e": {"value": nvis / e2e_s / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "cells": cells,
+    }
+
+
 def roofline(per, n, nx, P, sc, peak, peak_kind):
     ab = algorithmic_bytes(n, nx, nx, P, sc)
     med = {s: statistics.median(v) for s, v in per.items() if v}
@@ -468,6 +676,11 @@ def main():
 
     import torch
     peak, peak_kind = peaks()
+    if args.workload == "c4":
+        line = bench_batch(args, rank, world, peak, peak_kind)
+        if line is not None:
+            print(json.dumps(line))
+        return 0
     res, obs = bench_ours(args, rank, world)
     if rank != 0:
         return 0
@@ -496,7 +709,11 @@ def main():
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
         "roofline": {"bound": "hbm", "kernel": "gridding stage (bin_count+bin_scan+bin_scatter+grid)",
                      "achieved": g["gbs"], "peak": peak, "unit": "GB/s", "frac": g["frac"],
-                     "peak_source": f"{peak_kind} hbm copy bandwidth", "traffic": None,
+                     "peak_source": f"{peak_kind} hbm copy bandwidth",
+                     "traffic": profiled_traffic(res["stats"]["records"]),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                                       "stage's kernels (profiles/launches_fwd_adj_4096x32_50M.md),"
+                                       " scaled by records",
                      "algorithmic_bytes_per_launch": g["bytes"]},
         "stages": stages,
         "gpu_launches": args.steps * sum(OUR_KERNELS_PER_STEP.values()),

@@ -206,6 +206,79 @@ WSG_API int wsg_image_adjoint_host(wsg_plan *plan, const void *image, void *out)
 /* Resident grid of the plan ([P][Ny][Nx] complex), for inspection. */
 WSG_API void *wsg_plan_grid(wsg_plan *plan);
 
+/* Times candidate settings of the tile edge, split size and persistent CTA
+ * count on these inputs (wsg_image_forward, `iters` timed calls each after
+ * one warm-up, searched one parameter at a time) and keeps the fastest.
+ * best (optional) receives it; tried (optional, max_tried entries) every
+ * candidate timed, *n_tried their number. */
+typedef struct {
+    int tile, ctas, chunk;   /* as wsg_plan_set_tuning (ctas 0 = automatic) */
+    float ms;                /* mean time of one timed call                 */
+} wsg_tuning;
+WSG_API int wsg_plan_autotune(wsg_plan *plan, long num_points, long freq_per_chan,
+                              long polarizations, const double *uu, const double *vv,
+                              const double *ww, const float *vis_real, const float *vis_img,
+                              const float *weight, void *image, int iters, wsg_tuning *best,
+                              wsg_tuning *tried, int max_tried, int *n_tried);
+
+/* ------------------------------------------------------------------ */
+/* 3. (channel, polarisation) batches                                   */
+/* ------------------------------------------------------------------ */
+/*
+ * Many channels and polarisations imaged at once; the reference has no such
+ * entry point (it folds all freq_per_chan*polarizations into one grid,
+ * w-stacking.cu:98-112).  Each (channel, polarisation) pair is one job: the
+ * grid, FFT and w-corrected image that wstack() + fftw_data +
+ * phase_correction() give for that channel and polarisation alone
+ * (freq_per_chan = polarizations = 1).  Jobs share the grid geometry, dx,
+ * dw, the support and the w-correction geometry; each channel has its own
+ * uvw and measurement count (after flagging).  Layouts:
+ *   grids   [channel][pol][P][Ny][Nx] complex64 (job = channel*pols + pol)
+ *   images  [channel][pol][Ny][Nx] complex64
+ *   vis_out [sum over channels of num_points*pols] complex64, channel after
+ *           channel, each [num_points][pols] (wsg_batch_vis_offset)
+ * All jobs are binned in one pass and gridded in one persistent launch over a
+ * (job, plane, tile) work queue; the whole forward can be replayed as one
+ * CUDA graph.  WSG_FP32C only, power-of-two grid edges 256..8192.
+ */
+typedef struct wsg_batch wsg_batch;
+typedef struct {
+    long num_points;                   /* measurements of this channel (>= 0) */
+    const double *uu, *vv, *ww;        /* [num_points], device               */
+    const float *vis_real, *vis_img;   /* [num_points][pols], device          */
+    const float *weight;               /* [num_points][pols], device          */
+} wsg_channel;
+
+WSG_API int wsg_batch_create(wsg_batch **batch, int grid_size_x, int grid_size_y,
+                             int num_w_planes, int w_support, double dx, double dw,
+                             int num_channels, int polarizations, void *stream);
+WSG_API int wsg_batch_destroy(wsg_batch *batch);
+WSG_API int wsg_batch_set_stream(wsg_batch *batch, void *stream);
+WSG_API int wsg_batch_set_wcorrection(wsg_batch *batch, double resolution, double wmin,
+                                      double wmax);
+WSG_API int wsg_batch_set_tuning(wsg_batch *batch, int tile, int ctas, int chunk);
+/* Binds the channels' input buffers (num_channels entries; the table is
+ * copied, the buffers are not: they must stay allocated while bound, and
+ * their contents may change between forwards) and reserves device memory. */
+WSG_API int wsg_batch_bind(wsg_batch *batch, const wsg_channel *channels);
+/* Forward of every job into images (overwritten).  use_graph = 1 captures
+ * bin + grid + FFT + w-correction as one CUDA graph on first use and replays
+ * it while the binding, tuning, w-correction and images pointer stay the same. */
+WSG_API int wsg_batch_forward(wsg_batch *batch, void *images, int use_graph);
+/* Adjoint of the forward for the bound measurements (after a forward):
+ * vis_out = A^H images, per visibility as wsg_image_adjoint. */
+WSG_API int wsg_batch_adjoint(wsg_batch *batch, const void *images, void *vis_out);
+/* As wsg_plan_autotune, timing wsg_batch_forward on the bound inputs. */
+WSG_API int wsg_batch_autotune(wsg_batch *batch, void *images, int iters, wsg_tuning *best,
+                               wsg_tuning *tried, int max_tried, int *n_tried);
+/* First visibility of `channel` in vis_out; channel = num_channels gives the
+ * total (-1 before wsg_batch_bind). */
+WSG_API long long wsg_batch_vis_offset(wsg_batch *batch, int channel);
+/* Resident grids of the last forward ([channel][pol][P][Ny][Nx] complex64). */
+WSG_API void *wsg_batch_grids(wsg_batch *batch);
+WSG_API int wsg_batch_get_stats(wsg_batch *batch, wsg_stats *stats);
+WSG_API long long wsg_batch_device_bytes(wsg_batch *batch);
+
 /*
  * FP64 gridding that allocates no device memory.  It has no counterpart in
  * the reference; it is for callers that cannot call cudaMalloc when they grid

@@ -43,6 +43,17 @@ class Stats(ctypes.Structure):
                 ("ctas", ctypes.c_int)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_int), ("ctas", ctypes.c_int), ("chunk", ctypes.c_int),
+                ("ms", ctypes.c_float)]
+
+
+class Channel(ctypes.Structure):
+    _fields_ = [("num_points", ctypes.c_long), ("uu", ctypes.c_void_p), ("vv", ctypes.c_void_p),
+                ("ww", ctypes.c_void_p), ("vis_real", ctypes.c_void_p),
+                ("vis_img", ctypes.c_void_p), ("weight", ctypes.c_void_p)]
+
+
 _P = ctypes.c_void_p
 _D = ctypes.c_double
 _I = ctypes.c_int
@@ -79,6 +90,23 @@ SIGNATURES = {
     "wsg_image_adjoint": (_I, [_P, _P, _P]),
     "wsg_image_forward_host": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
     "wsg_image_adjoint_host": (_I, [_P, _P, _P]),
+    "wsg_plan_autotune": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P, _I,
+                               ctypes.POINTER(Tuning), ctypes.POINTER(Tuning), _I,
+                               ctypes.POINTER(_I)]),
+    "wsg_batch_create": (_I, [ctypes.POINTER(_P), _I, _I, _I, _I, _D, _D, _I, _I, _P]),
+    "wsg_batch_destroy": (_I, [_P]),
+    "wsg_batch_set_stream": (_I, [_P, _P]),
+    "wsg_batch_set_wcorrection": (_I, [_P, _D, _D, _D]),
+    "wsg_batch_set_tuning": (_I, [_P, _I, _I, _I]),
+    "wsg_batch_bind": (_I, [_P, ctypes.POINTER(Channel)]),
+    "wsg_batch_forward": (_I, [_P, _P, _I]),
+    "wsg_batch_adjoint": (_I, [_P, _P, _P]),
+    "wsg_batch_autotune": (_I, [_P, _P, _I, ctypes.POINTER(Tuning), ctypes.POINTER(Tuning), _I,
+                                ctypes.POINTER(_I)]),
+    "wsg_batch_vis_offset": (ctypes.c_longlong, [_P, _I]),
+    "wsg_batch_grids": (_P, [_P]),
+    "wsg_batch_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
+    "wsg_batch_device_bytes": (ctypes.c_longlong, [_P]),
     "wsg_grid_noalloc": (_I, [_I, _L, _L, _L, _P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P, _P]),
 }
 

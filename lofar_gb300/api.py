@@ -267,3 +267,167 @@ class Plan:
         self._sync_stream()
         check(self.lib.wsg_image_adjoint_host(self._h, _ptr(image), _ptr(out)))
         return out
+
+    # -- tuning ---------------------------------------------------------------
+    def autotune(self, uu, vv, ww, vis_real, vis_img, weight, iters: int = 3, freq_per_chan=1,
+                 polarizations=1, image=None):
+        """Time tile/split/CTA candidates on these inputs (forward imaging) and
+        keep the fastest; returns (best, tried) as dicts."""
+        ins = self._inputs(uu, vv, ww, vis_real, vis_img, weight)
+        n = ins[0].numel()
+        image = self._torch.empty((self.ny, self.nx), dtype=self.cdtype, device="cuda") if image is None else image
+        best = _lib.Tuning()
+        tried = (_lib.Tuning * 64)()
+        nt = ctypes.c_int(0)
+        self._sync_stream()
+        check(self.lib.wsg_plan_autotune(self._h, n, int(freq_per_chan), int(polarizations),
+                                         *[x.data_ptr() for x in ins], image.data_ptr(), int(iters),
+                                         ctypes.byref(best), tried, 64, ctypes.byref(nt)))
+        self._keep = ins
+        self.n_binned = n
+        return _tuning_dict(best), [_tuning_dict(tried[i]) for i in range(min(nt.value, 64))]
+
+
+def _tuning_dict(t) -> dict:
+    return {"tile": t.tile, "ctas": t.ctas, "chunk": t.chunk, "ms": t.ms}
+
+
+class Batch:
+    """Many (channel, polarisation) jobs imaged together (FP32C).
+
+    Each job is what wstack() + FFT + phase_correction() give for one channel
+    and one polarisation alone.  Channels share the grid geometry and the
+    w-correction; each has its own uvw and measurement count.  Inputs per
+    channel c: uu, vv, ww float64 [n_c]; vis_real, vis_img, weight float32
+    [n_c][pols].  Outputs: images [channels][pols][ny][nx] complex64; the
+    adjoint gives one complex64 per visibility, channel after channel.
+    """
+
+    def __init__(self, nx: int, ny: int, planes: int, support: int, channels: int, pols: int,
+                 dx: float | None = None, dw: float | None = None):
+        import torch
+        self._torch = torch
+        self.nx, self.ny, self.planes, self.support = int(nx), int(ny), int(planes), int(support)
+        self.channels, self.pols = int(channels), int(pols)
+        self.dx = 1.0 / nx if dx is None else float(dx)
+        self.dw = 1.0 / planes if dw is None else float(dw)
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self.lib.wsg_batch_create(ctypes.byref(h), self.nx, self.ny, self.planes,
+                                        self.support, self.dx, self.dw, self.channels, self.pols,
+                                        self._stream()))
+        self._h = h
+        self._bound = None
+
+    def _stream(self):
+        return ctypes.c_void_p(self._torch.cuda.current_stream().cuda_stream)
+
+    def _sync_stream(self):
+        check(self.lib.wsg_batch_set_stream(self._h, self._stream()))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.lib.wsg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_wcorrection(self, resolution: float, wmin: float, wmax: float):
+        check(self.lib.wsg_batch_set_wcorrection(self._h, float(resolution), float(wmin),
+                                                 float(wmax)))
+
+    def set_tuning(self, tile: int = 0, ctas: int = 0, chunk: int = 0):
+        check(self.lib.wsg_batch_set_tuning(self._h, int(tile), int(ctas), int(chunk)))
+
+    def bind(self, channels):
+        """channels: sequence of (uu, vv, ww, vis_real, vis_img, weight) per channel."""
+        if len(channels) != self.channels:
+            raise ValueError(f"expected {self.channels} channels, got {len(channels)}")
+        t = self._torch
+        dev = t.device("cuda", t.cuda.current_device())
+        keep = []
+        table = (_lib.Channel * self.channels)()
+        for c, (uu, vv, ww, vr, vi, wt) in enumerate(channels):
+            ins = [t.as_tensor(x, dtype=dt, device=dev).contiguous()
+                   for x, dt in ((uu, t.float64), (vv, t.float64), (ww, t.float64),
+                                 (vr, t.float32), (vi, t.float32), (wt, t.float32))]
+            n = ins[0].numel()
+            for x in ins[3:]:
+                if x.numel() != n * self.pols:
+                    raise ValueError(f"channel {c}: vis/weight need {n}x{self.pols} entries")
+            table[c] = _lib.Channel(n, *[x.data_ptr() for x in ins])
+            keep.append(ins)
+        self._sync_stream()
+        check(self.lib.wsg_batch_bind(self._h, table))
+        self._bound = keep
+        return self
+
+    def new_images(self):
+        return self._torch.empty((self.channels, self.pols, self.ny, self.nx),
+                                 dtype=self._torch.complex64, device="cuda")
+
+    def forward(self, images=None, graph: bool = True):
+        images = self.new_images() if images is None else images
+        assert images.dtype == self._torch.complex64 and images.is_contiguous()
+        assert images.numel() == self.channels * self.pols * self.ny * self.nx
+        self._sync_stream()
+        check(self.lib.wsg_batch_forward(self._h, images.data_ptr(), int(bool(graph))))
+        return images
+
+    def n_vis(self) -> int:
+        return int(self.lib.wsg_batch_vis_offset(self._h, self.channels))
+
+    def vis_offset(self, channel: int) -> int:
+        return int(self.lib.wsg_batch_vis_offset(self._h, int(channel)))
+
+    def adjoint(self, images, out=None):
+        images = images.to(self._torch.complex64).contiguous()
+        out = self._torch.empty(self.n_vis(), dtype=self._torch.complex64, device="cuda") if out is None else out
+        self._sync_stream()
+        check(self.lib.wsg_batch_adjoint(self._h, images.data_ptr(), out.data_ptr()))
+        return out
+
+    def grids(self):
+        """View of the resident grids [channels][pols][P][ny][nx] (complex64)."""
+        ptr = self.lib.wsg_batch_grids(self._h)
+        return _wrap_device(ptr, (self.channels, self.pols, self.planes, self.ny, self.nx),
+                            self._torch.complex64)
+
+    def autotune(self, images=None, iters: int = 3):
+        images = self.new_images() if images is None else images
+        best = _lib.Tuning()
+        tried = (_lib.Tuning * 64)()
+        nt = ctypes.c_int(0)
+        self._sync_stream()
+        check(self.lib.wsg_batch_autotune(self._h, images.data_ptr(), int(iters),
+                                          ctypes.byref(best), tried, 64, ctypes.byref(nt)))
+        return _tuning_dict(best), [_tuning_dict(tried[i]) for i in range(min(nt.value, 64))]
+
+    def stats(self) -> dict:
+        self._sync_stream()
+        s = _lib.Stats()
+        check(self.lib.wsg_batch_get_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+
+    def device_bytes(self) -> int:
+        return int(self.lib.wsg_batch_device_bytes(self._h))
+
+
+class _DevArray:
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def _wrap_device(ptr, shape, dtype):
+    """A torch tensor viewing library-owned device memory (valid while the owner lives)."""
+    import torch
+    if not ptr:
+        raise WstackError(_lib.WSG_ERR_STATE, "no device buffer")
+    typestr = {torch.complex64: "<f4", torch.complex128: "<f8"}[dtype]
+    real = torch.as_tensor(_DevArray(ptr, tuple(shape) + (2,), typestr), device="cuda")
+    return torch.view_as_complex(real)

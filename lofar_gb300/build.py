@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwstack_gb300.so")
 
-SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "capi.cu", "batch.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -10,6 +10,8 @@
 //   k_bin_scan_c   per-bin record offsets; bins above the split size are cut
 //                  into work items of at most that many records
 //   k_bin_scatter  second pass over all inputs: writes the records
+// k_bin_count_batch / k_bin_scatter_batch replace the two passes for a
+// (channel, polarisation) batch, whose jobs are stacked along the plane axis.
 // The tile kernels take the split items first, then every other bin, so no
 // work item holds more than `split` records and the load stays balanced.
 #include <cuda_runtime.h>
@@ -48,7 +50,7 @@ __device__ __forceinline__ int measure(const GeomParams &g, double x, double y, 
     const int ju0 = max(cu.g - K, 0), ju1 = min(cu.g + K, g.nx - 1);
     const int jv0 = max(cv.g - K, 0), jv1 = min(cv.g + K, g.ny - 1);
     if (ju0 > ju1 || jv0 > jv1) return 2;
-    if (!cw.ok || cw.g < 0 || cw.g >= g.planes) return 1;
+    if (!cw.ok || cw.g < 0 || cw.g >= g.wplanes) return 1;
     o.gu = cu.g;
     o.gv = cv.g;
     o.gw = cw.g;
@@ -224,6 +226,158 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
                                                   __float_as_uint((float)im));
                     }
                     r.idx[pos] = (unsigned)m;
+                }
+            }
+        }
+    }
+}
+
+// ---- (channel, polarisation) batches ----------------------------------------
+//
+// One pass over the concatenated measurements of all channels.  A
+// measurement's coordinates are computed once; each polarisation p gives its
+// own records, in the bins of job c*pols + p (cube plane job*P + w).  Every
+// job is what the reference's wstack() computes for that channel and
+// polarisation alone (freq_per_chan = polarizations = 1, w-stacking.cu:98-112
+// with one entry): the record value is the float product weight*vis, zero
+// where vis_real is NaN.
+
+// Largest c with m0[c] <= m: the channel holding global measurement m (empty
+// channels share their successor's m0 and are skipped).
+__device__ __forceinline__ int chan_of(const long long *s_m0, int nch, long long m)
+{
+    int lo = 0, hi = nch - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_m0[mid] <= m) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+struct BatchPoint {
+    const float *vr, *vi, *wt;
+    long long e0;                 // [m][pols] index of polarisation 0
+    unsigned long long vis0;
+    int c;
+};
+
+template <bool UP2, bool WP2, typename F>
+__device__ __forceinline__ int batch_point(const GeomParams &g, const ChanTable &t,
+                                           const long long *s_m0, long long m, MGeom &o,
+                                           F &fu, F &fv, BatchPoint &bp)
+{
+    if (m >= t.ntot) return 3;
+    const int c = chan_of(s_m0, t.nch, m);
+    const ChanDesc *d = t.ch + c;
+    const long long ml = m - s_m0[c];
+    bp.c = c;
+    bp.vr = d->vr;
+    bp.vi = d->vi;
+    bp.wt = d->wt;
+    bp.e0 = ml * t.pols;
+    bp.vis0 = d->vis0;
+    return measure<UP2, WP2, F>(g, __ldcs(d->uu + ml), __ldcs(d->vv + ml), __ldcs(d->ww + ml), o,
+                                fu, fv);
+}
+
+template <bool UP2, bool WP2>
+__global__ void __launch_bounds__(256) k_bin_count_batch(GeomParams g, ChanTable t, BinBuffers b)
+{
+    __shared__ long long s_m0[kMaxChannels];
+    for (int i = threadIdx.x; i < t.nch; i += blockDim.x) s_m0[i] = t.m0[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nb = g.nbins;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < t.ntot; base += stride) {
+        const long long m = base + threadIdx.x;
+        MGeom o;
+        float fu, fv;
+        BatchPoint bp;
+        const int st = batch_point<UP2, WP2, float>(g, t, s_m0, m, o, fu, fv, bp);
+        const unsigned sub = sub_of(m);
+        for (int p = 0; p < t.pols; p++) {
+            const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
+            const unsigned prim = (st == 0) ? bin_index(g, plane, o.tvp, o.tup) : kFull;
+            const unsigned peers = __match_any_sync(kFull, prim);
+            if (st == 0) {
+                if (lane == __ffs(peers) - 1)
+                    atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
+                for (int tv = o.tv0; tv <= o.tv1; tv++)
+                    for (int tu = o.tu0; tu <= o.tu1; tu++)
+                        if (tv != o.tvp || tu != o.tup)
+                            atomicAdd(&b.sub_dup[sub * nb + bin_index(g, plane, tv, tu)], 1u);
+            }
+        }
+        int ndp = st == 1, ndw = st == 2;
+        for (int d = 16; d >= 1; d >>= 1) {
+            ndp += __shfl_xor_sync(kFull, ndp, d);
+            ndw += __shfl_xor_sync(kFull, ndw, d);
+        }
+        if (lane == 0) {
+            if (ndp) atomicAdd(&b.ctr->dropped_plane, (unsigned long long)ndp);
+            if (ndw) atomicAdd(&b.ctr->dropped_window, (unsigned long long)ndw);
+        }
+    }
+}
+
+template <bool UP2, bool WP2, int PREC>
+__global__ void __launch_bounds__(256)
+k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
+{
+    using S = typename std::conditional<PREC == WSG_FP64, double, float>::type;
+    __shared__ long long s_m0[kMaxChannels];
+    for (int i = threadIdx.x; i < t.nch; i += blockDim.x) s_m0[i] = t.m0[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nb = g.nbins;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < t.ntot; base += stride) {
+        const long long m = base + threadIdx.x;
+        MGeom o;
+        S fu, fv;
+        BatchPoint bp;
+        const int st = batch_point<UP2, WP2, S>(g, t, s_m0, m, o, fu, fv, bp);
+        const unsigned sub = sub_of(m);
+        for (int p = 0; p < t.pols; p++) {
+            const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
+            const unsigned prim = (st == 0) ? bin_index(g, plane, o.tvp, o.tup) : kFull;
+            const unsigned peers = __match_any_sync(kFull, prim);
+            const int leader = __ffs(peers) - 1;
+            unsigned got = 0;
+            if (st == 0 && lane == leader)
+                got = atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
+            const unsigned basep = __shfl_sync(kFull, got, leader);
+            if (st != 0) continue;
+            const unsigned ppos = basep + (unsigned)__popc(peers & lt_mask);
+            const long long e = bp.e0 + p;
+            const float a = __ldcs(bp.vr + e);
+            S re = 0, im = 0;
+            if (!isnan(a)) {
+                const float w = __ldcs(bp.wt + e);
+                re = (S)(w * a);
+                im = (S)(w * __ldcs(bp.vi + e));
+            }
+            const unsigned idx = (unsigned)(bp.vis0 + (unsigned long long)e);
+            for (int tv = o.tv0; tv <= o.tv1; tv++) {
+                for (int tu = o.tu0; tu <= o.tu1; tu++) {
+                    const bool primary = tv == o.tvp && tu == o.tup;
+                    const unsigned pos =
+                        primary ? ppos : atomicAdd(&b.sub_dup[sub * nb + bin_index(g, plane, tv, tu)], 1u);
+                    const int cu = o.gu - tu * g.tile;
+                    const int cv = o.gv - tv * g.tile;
+                    if (PREC == WSG_FP64) {
+                        r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
+                        reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu, fv);
+                        reinterpret_cast<double2 *>(r.val)[pos] = make_double2(re, im);
+                    } else {
+                        r.rec16[pos] = make_uint4(pack_axis(cu, (float)fu), pack_axis(cv, (float)fv),
+                                                  __float_as_uint((float)re),
+                                                  __float_as_uint((float)im));
+                    }
+                    r.idx[pos] = idx;
                 }
             }
         }
@@ -483,6 +637,46 @@ cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu, 
     if (n <= 0) return cudaSuccess;
     if (prec == WSG_FP64) scatter_dispatch<WSG_FP64>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r, s);
     else scatter_dispatch<WSG_FP32C>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r, s);
+    return cudaGetLastError();
+}
+
+template <int PREC>
+static void scatter_batch_dispatch(const GeomParams &g, const ChanTable &t, const BinBuffers &b,
+                                   const RecBuffers &r, int blocks, cudaStream_t s)
+{
+    if (g.u_pow2 && g.w_pow2) k_bin_scatter_batch<true, true, PREC><<<blocks, 256, 0, s>>>(g, t, b, r);
+    else if (g.u_pow2) k_bin_scatter_batch<true, false, PREC><<<blocks, 256, 0, s>>>(g, t, b, r);
+    else if (g.w_pow2) k_bin_scatter_batch<false, true, PREC><<<blocks, 256, 0, s>>>(g, t, b, r);
+    else k_bin_scatter_batch<false, false, PREC><<<blocks, 256, 0, s>>>(g, t, b, r);
+}
+
+static int batch_blocks(long long n)
+{
+    const long long want = (n + 255) / 256;
+    return (int)max(1ll, min(want, (long long)num_sms() * 8));
+}
+
+cudaError_t launch_bin_count_batch(const GeomParams &g, const ChanTable &t, const BinBuffers &b,
+                                   cudaStream_t s)
+{
+    if (t.ntot <= 0) return cudaSuccess;
+    if (t.nch <= 0 || t.nch > kMaxChannels) return cudaErrorInvalidValue;
+    const int blocks = batch_blocks(t.ntot);
+    if (g.u_pow2 && g.w_pow2) k_bin_count_batch<true, true><<<blocks, 256, 0, s>>>(g, t, b);
+    else if (g.u_pow2) k_bin_count_batch<true, false><<<blocks, 256, 0, s>>>(g, t, b);
+    else if (g.w_pow2) k_bin_count_batch<false, true><<<blocks, 256, 0, s>>>(g, t, b);
+    else k_bin_count_batch<false, false><<<blocks, 256, 0, s>>>(g, t, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_scatter_batch(const GeomParams &g, int prec, const ChanTable &t,
+                                     const BinBuffers &b, const RecBuffers &r, cudaStream_t s)
+{
+    if (t.ntot <= 0) return cudaSuccess;
+    if (t.nch <= 0 || t.nch > kMaxChannels) return cudaErrorInvalidValue;
+    const int blocks = batch_blocks(t.ntot);
+    if (prec == WSG_FP64) scatter_batch_dispatch<WSG_FP64>(g, t, b, r, blocks, s);
+    else scatter_batch_dispatch<WSG_FP32C>(g, t, b, r, blocks, s);
     return cudaGetLastError();
 }
 

@@ -11,20 +11,20 @@
 #include <mutex>
 #include <new>
 
-#include "wsg_internal.cuh"
+#include "plan.cuh"
 
 using namespace wsg;
 
 // ---------------------------------------------------------------------------
-// error state
+// error state and shared helpers
 // ---------------------------------------------------------------------------
 
 namespace {
-
 thread_local int tl_status = WSG_OK;
 thread_local char tl_msg[512] = "";
+}  // namespace
 
-int set_error(int status, const char *fmt, ...)
+int wsg::set_error(int status, const char *fmt, ...)
 {
     tl_status = status;
     va_list ap;
@@ -34,64 +34,15 @@ int set_error(int status, const char *fmt, ...)
     return status;
 }
 
-int clear_error()
+int wsg::clear_error()
 {
     tl_status = WSG_OK;
     tl_msg[0] = 0;
     return WSG_OK;
 }
 
-#define WSG_CUDA(call)                                                                  \
-    do {                                                                                \
-        cudaError_t e_ = (call);                                                        \
-        if (e_ != cudaSuccess) {                                                        \
-            return set_error(e_ == cudaErrorMemoryAllocation ? WSG_ERR_NOMEM : WSG_ERR_CUDA, \
-                             "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__,    \
-                             __LINE__);                                                 \
-        }                                                                               \
-    } while (0)
-
-#define WSG_CUFFT(call)                                                                 \
-    do {                                                                                \
-        cufftResult r_ = (call);                                                        \
-        if (r_ != CUFFT_SUCCESS)                                                        \
-            return set_error(WSG_ERR_CUFFT, "%s: cufft status %d (%s:%d)", #call, (int)r_,  \
-                             __FILE__, __LINE__);                                       \
-    } while (0)
-
-#define WSG_TRY(call)                 \
-    do {                              \
-        int s_ = (call);              \
-        if (s_ != WSG_OK) return s_;  \
-    } while (0)
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t n)
-    {
-        if (n <= bytes && p) return cudaSuccess;
-        release();
-        cudaError_t e = cudaMalloc(&p, n ? n : 16);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return e;
-        }
-        bytes = n ? n : 16;
-        return cudaSuccess;
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
-};
-
-bool is_pow2_recip(double d, int &k)
+bool wsg::is_pow2_recip(double d, int &k)
 {
-    // d == 2^-k exactly, 0 <= k <= 1000
     if (!(d > 0.0) || !isfinite(d)) return false;
     int e;
     const double m = frexp(d, &e);
@@ -100,7 +51,7 @@ bool is_pow2_recip(double d, int &k)
     return k >= 0 && k <= 1000;
 }
 
-bool device_accessible(const void *ptr)
+bool wsg::device_accessible(const void *ptr)
 {
     if (!ptr) return false;
     cudaPointerAttributes a;
@@ -110,8 +61,6 @@ bool device_accessible(const void *ptr)
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
-
-}  // namespace
 
 // Records a status and message as this thread's last error (for entry points
 // defined in other translation units).
@@ -138,65 +87,7 @@ int wsg::num_sms()
 // plan
 // ---------------------------------------------------------------------------
 
-struct wsg_plan {
-    int nx, ny, planes, support, half, prec;
-    double dx, dw;
-    cudaStream_t stream = nullptr;
-    int tile = 64, ctas_grid = 0, ctas_degrid = 0, split = kDefaultSplit, ctas_user = 0;
-    GeomParams geom{};
-
-    DevBuf grid;                          // resident [P][Ny][Nx] complex
-    DevBuf bins;                          // bin_buffer_bytes(nbins)
-    DevBuf ctr;                           // DevCounters
-    DevBuf rec16, rcell, rfrac, rval, ridx;   // records (FP32C: rec16+idx; FP64: SoA)
-    DevBuf partials;                      // FP32C partial tiles of split bins
-    unsigned long long rec_cap = 0;
-    long long n_binned = -1;
-
-    // staging for *_host calls
-    DevBuf h_uu, h_vv, h_ww, h_vr, h_vi, h_wt, h_image, h_out;
-
-    bool wc_set = false, ws_ready = false;
-    WcParams wc{};
-    DevBuf sinx, siny, wscreen;
-
-    cufftHandle fft = 0;
-    bool fft_ready = false;
-    int fft_batch = 0;
-    DevBuf fft_work;
-
-    // FP32C fused FFT + w-correction (power-of-two grids)
-    bool fused = false;
-    bool tw_ready = false;
-    bool masks_valid = false;
-    DevBuf twx, twy, masks;
-
-    size_t elem() const { return prec == WSG_FP64 ? sizeof(double2) : sizeof(float2); }
-    long long npix() const { return (long long)nx * ny; }
-    BinBuffers binbufs() const
-    {
-        BinBuffers b;
-        bin_buffer_carve(bins.p, geom.nbins, b);
-        b.ctr = ctr.as<DevCounters>();
-        b.split_size = (unsigned)split;
-        return b;
-    }
-    RecBuffers recbufs() const
-    {
-        RecBuffers r;
-        r.rec16 = rec16.as<uint4>();
-        r.cell = rcell.as<unsigned>();
-        r.frac = rfrac.p;
-        r.val = rval.p;
-        r.idx = ridx.as<unsigned>();
-        r.capacity = rec_cap;
-        return r;
-    }
-};
-
-namespace {
-
-WScreen wsg_plan_wscreen(const wsg_plan *p)
+WScreen wsg::plan_wscreen(const wsg_plan *p)
 {
     WScreen ws;
     float *base = p->wscreen.as<float>();
@@ -211,17 +102,18 @@ WScreen wsg_plan_wscreen(const wsg_plan *p)
     return ws;
 }
 
-int plan_configure(wsg_plan *p)
+int wsg::plan_configure(wsg_plan *p)
 {
     GeomParams &g = p->geom;
     g.nx = p->nx;
     g.ny = p->ny;
-    g.planes = p->planes;
     g.half = p->half;
     g.tile = p->tile;
     g.ntu = (p->nx + p->tile - 1) / p->tile;
     g.ntv = (p->ny + p->tile - 1) / p->tile;
-    g.nbins = (long long)p->planes * g.ntv * g.ntu;
+    g.wplanes = p->planes;
+    g.planes = (int)p->cube_planes();
+    g.nbins = p->cube_planes() * g.ntv * g.ntu;
     g.dx = p->dx;
     g.dw = p->dw;
     int k = 0;
@@ -248,7 +140,7 @@ int plan_configure(wsg_plan *p)
     return WSG_OK;
 }
 
-int ensure_records(wsg_plan *p, long long n)
+int wsg::ensure_records(wsg_plan *p, long long n)
 {
     // a support window of <= tile cells touches at most 2x2 tiles
     const unsigned long long need = (unsigned long long)(n > 0 ? n : 1) * 4ull;
@@ -268,6 +160,8 @@ int ensure_records(wsg_plan *p, long long n)
     p->rec_cap = need;
     return WSG_OK;
 }
+
+namespace {
 
 int ensure_fft(wsg_plan *p)
 {
@@ -300,22 +194,24 @@ int ensure_fft(wsg_plan *p)
     return WSG_OK;
 }
 
-FftMasks mask_view(const wsg_plan *p)
+}  // namespace
+
+FftMasks wsg::mask_view(const wsg_plan *p)
 {
     FftMasks m;
-    const size_t nt = (size_t)p->planes * p->geom.ntv * p->geom.ntu;
-    const size_t nc = (size_t)p->planes * p->geom.ntu;
+    const size_t nt = (size_t)p->cube_planes() * p->geom.ntv * p->geom.ntu;
+    const size_t nc = (size_t)p->cube_planes() * p->geom.ntu;
     unsigned char *b = p->masks.as<unsigned char>();
     m.occ_tile = b;
     m.need_tile = b + nt;
     m.occ_col = b + 2 * nt;
     m.need_col = b + 2 * nt + nc;
     m.plane_occ = b + 2 * nt + 2 * nc;
-    m.plane_need = b + 2 * nt + 2 * nc + p->planes;
+    m.plane_need = b + 2 * nt + 2 * nc + p->cube_planes();
     return m;
 }
 
-int ensure_fused(wsg_plan *p)
+int wsg::ensure_fused(wsg_plan *p)
 {
     if (!p->tw_ready) {
         WSG_CUDA(p->twx.ensure(sizeof(float2) * p->nx));
@@ -324,13 +220,13 @@ int ensure_fused(wsg_plan *p)
         WSG_CUDA(launch_twiddles(p->twy.as<float2>(), p->ny, p->stream));
         p->tw_ready = true;
     }
-    const size_t nt = (size_t)p->planes * p->geom.ntv * p->geom.ntu;
-    const size_t nc = (size_t)p->planes * p->geom.ntu;
-    WSG_CUDA(p->masks.ensure(2 * nt + 2 * nc + 2 * (size_t)p->planes));
+    const size_t nt = (size_t)p->cube_planes() * p->geom.ntv * p->geom.ntu;
+    const size_t nc = (size_t)p->cube_planes() * p->geom.ntu;
+    WSG_CUDA(p->masks.ensure(2 * nt + 2 * nc + 2 * (size_t)p->cube_planes()));
     return WSG_OK;
 }
 
-int ensure_wscreen(wsg_plan *p)
+int wsg::ensure_wscreen(wsg_plan *p)
 {
     if (!p->wc_set) return set_error(WSG_ERR_STATE, "w-correction geometry not set");
     if (p->ws_ready) return WSG_OK;
@@ -339,13 +235,22 @@ int ensure_wscreen(wsg_plan *p)
     WSG_CUDA(launch_wscreen_tables(p->wc, p->sinx.as<double>(), p->siny.as<double>(), p->stream));
     if (p->prec == WSG_FP32C && p->wc.phase_on && p->planes > 1) {
         WSG_CUDA(p->wscreen.ensure(sizeof(float) * 5 * (size_t)p->npix()));
-        WSG_CUDA(launch_wscreen_build(p->wc, wsg_plan_wscreen(p), p->stream));
+        WSG_CUDA(launch_wscreen_build(p->wc, plan_wscreen(p), p->stream));
     }
     p->ws_ready = true;
     return WSG_OK;
 }
 
-}  // namespace
+int wsg::finish_binning(wsg_plan *p)
+{
+    p->masks_valid = false;
+    if (p->fused) {
+        WSG_TRY(ensure_fused(p));
+        WSG_CUDA(launch_fft_masks(p->geom, p->binbufs(), mask_view(p), p->stream));
+        p->masks_valid = true;
+    }
+    return WSG_OK;
+}
 
 
 extern "C" {
@@ -438,7 +343,7 @@ int wsg_plan_reserve(wsg_plan *p, long max_points)
     if (max_points < 0 || max_points > 1000000000L)
         return set_error(WSG_ERR_UNSUPPORTED, "max_points outside [0, 1e9]");
     WSG_TRY(ensure_records(p, max_points));
-    WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->planes * p->npix()));
+    WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->cube_planes() * p->npix()));
     WSG_TRY(ensure_fft(p));
     return WSG_OK;
 }
@@ -500,6 +405,7 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
 {
     clear_error();
     if (!p) return set_error(WSG_ERR_ARG, "plan is NULL");
+    if (p->jobs != 1) return set_error(WSG_ERR_STATE, "a batch plan is binned by wsg_batch_bind");
     if (n < 0 || nf <= 0 || np <= 0) return set_error(WSG_ERR_ARG, "bad measurement counts");
     if (n > 1000000000L) return set_error(WSG_ERR_UNSUPPORTED, "more than 1e9 measurements");
     if (n > 0 && (!uu || !vv || !ww || !vr || !vi || !wt))
@@ -513,13 +419,7 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
     WSG_CUDA(launch_bin_scatter(p->geom, p->prec, uu, vv, ww, vr, vi, wt, n, nf, np, b,
                                 p->recbufs(), p->stream));
     p->n_binned = n;
-    p->masks_valid = false;
-    if (p->fused) {
-        WSG_TRY(ensure_fused(p));
-        WSG_CUDA(launch_fft_masks(p->geom, b, mask_view(p), p->stream));
-        p->masks_valid = true;
-    }
-    return WSG_OK;
+    return finish_binning(p);
 }
 
 int wsg_grid(wsg_plan *p, void *grid)
@@ -572,7 +472,7 @@ int wsg_wcorrect(wsg_plan *p, const void *planes, void *image, double scale)
                                      reinterpret_cast<double2 *>(image), nullptr, nullptr, scale,
                                      p->stream));
     } else {
-        WSG_CUDA(launch_wcorrect_f32c(p->wc, wsg_plan_wscreen(p),
+        WSG_CUDA(launch_wcorrect_f32c(p->wc, plan_wscreen(p),
                                       reinterpret_cast<const float2 *>(planes),
                                       reinterpret_cast<float2 *>(image), scale, p->stream));
     }
@@ -589,7 +489,7 @@ int wsg_wcorrect_adjoint(wsg_plan *p, const void *image, void *planes, double sc
                                          reinterpret_cast<const double2 *>(image),
                                          reinterpret_cast<double2 *>(planes), scale, p->stream));
     } else {
-        WSG_CUDA(launch_wcorrect_adj_f32c(p->wc, wsg_plan_wscreen(p),
+        WSG_CUDA(launch_wcorrect_adj_f32c(p->wc, plan_wscreen(p),
                                           reinterpret_cast<const float2 *>(image),
                                           reinterpret_cast<float2 *>(planes), scale, p->stream));
     }
@@ -631,7 +531,7 @@ int wsg_fft_wcorrect(wsg_plan *p, void *grid, void *image, int prune)
     }
     WSG_CUDA(launch_image_fwd_fused(p->geom, reinterpret_cast<float2 *>(grid),
                                     reinterpret_cast<float2 *>(image), p->twx.as<float2>(),
-                                    p->twy.as<float2>(), wsg_plan_wscreen(p), mask_view(p),
+                                    p->twy.as<float2>(), plan_wscreen(p), mask_view(p),
                                     p->wc.phase_on && p->planes > 1, scale, p->stream));
     return WSG_OK;
 }
@@ -651,7 +551,7 @@ int wsg_wcorrect_adjoint_fft(wsg_plan *p, const void *image, void *grid, int pru
     if (!p->masks_valid) return set_error(WSG_ERR_STATE, "pruned transform before wsg_bin");
     WSG_CUDA(launch_image_adj_fused(p->geom, reinterpret_cast<const float2 *>(image),
                                     reinterpret_cast<float2 *>(grid), p->twx.as<float2>(),
-                                    p->twy.as<float2>(), wsg_plan_wscreen(p), mask_view(p),
+                                    p->twy.as<float2>(), plan_wscreen(p), mask_view(p),
                                     p->wc.phase_on && p->planes > 1, scale, p->stream));
     return WSG_OK;
 }
@@ -662,7 +562,7 @@ int wsg_image_forward(wsg_plan *p, long n, long nf, long np, const double *uu, c
 {
     clear_error();
     if (!p || !image) return set_error(WSG_ERR_ARG, "NULL argument");
-    WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->planes * p->npix()));
+    WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->cube_planes() * p->npix()));
     WSG_TRY(ensure_wscreen(p));
     WSG_TRY(wsg_bin(p, n, nf, np, uu, vv, ww, vr, vi, wt));
     WSG_TRY(wsg_grid(p, p->grid.p));
@@ -675,7 +575,7 @@ int wsg_image_adjoint(wsg_plan *p, const void *image, void *out)
     clear_error();
     if (!p || !image) return set_error(WSG_ERR_ARG, "NULL argument");
     if (p->n_binned < 0) return set_error(WSG_ERR_STATE, "adjoint before a forward/bin call");
-    WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->planes * p->npix()));
+    WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->cube_planes() * p->npix()));
     WSG_TRY(wsg_wcorrect_adjoint_fft(p, image, p->grid.p, 1));
     WSG_TRY(wsg_degrid(p, p->grid.p, out));
     return WSG_OK;

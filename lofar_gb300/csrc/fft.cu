@@ -313,10 +313,10 @@ __global__ void __launch_bounds__(col_group<N>() * fft_threads<N>()) k_cols(ColA
 }
 
 struct RowArgs {
-    float2 *grid;     // [P][ny][nx]
-    float2 *image;    // [ny][nx]
+    float2 *grid;     // [jobs][P][ny][nx]
+    float2 *image;    // [jobs][ny][nx]
     const float2 *tw;
-    int nx, ny, planes, tile, ntu, phase, tsh;
+    int nx, ny, planes, tile, ntu, phase, tsh;   // planes: P, of one job
     WScreen ws;
     float scale;
     FftMasks m;
@@ -348,6 +348,11 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
     float *wal = wah + N, *wbh = wal + N, *wbl = wbh + N;
     const int y = blockIdx.x, t = threadIdx.x;
     const size_t prow = (size_t)y * N;
+    // job blockIdx.y: its planes, masks and image
+    const size_t jp = (size_t)blockIdx.y * a.planes;
+    const float2 *gridj = a.grid + jp * a.ny * N;
+    const unsigned char *plane_occ = a.m.plane_occ + jp;
+    float2 *image = a.image + (size_t)blockIdx.y * a.ny * N;
     if (a.phase) {
         for (int x = t; x < N; x += T) {
             wah[x] = a.ws.ah[prow + x];
@@ -357,7 +362,7 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
         }
     }
     unsigned char *smask = reinterpret_cast<unsigned char *>(wbl + N);   // [planes][ntu]
-    for (int i = t; i < a.planes * a.ntu; i += T) smask[i] = a.m.occ_col[i];
+    for (int i = t; i < a.planes * a.ntu; i += T) smask[i] = a.m.occ_col[jp * a.ntu + i];
     __syncthreads();
     float sr[Q], si[Q];
 #pragma unroll
@@ -365,10 +370,10 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
     // the next occupied plane's row is loaded into registers while the
     // current one is transformed
     int w = 0;
-    while (w < a.planes && !a.m.plane_occ[w]) w++;
+    while (w < a.planes && !plane_occ[w]) w++;
     float2 nxt[Q];
     auto fetch = [&](int ww) {
-        const float2 *src = a.grid + ((size_t)ww * a.ny + y) * N;
+        const float2 *src = gridj + ((size_t)ww * a.ny + y) * N;
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const int x = t + q * T;
@@ -381,7 +386,7 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
 #pragma unroll
         for (int q = 0; q < Q; q++) buf[pidx(t + q * T)] = nxt[q];
         int wn = w + 1;
-        while (wn < a.planes && !a.m.plane_occ[wn]) wn++;
+        while (wn < a.planes && !plane_occ[wn]) wn++;
         if (wn < a.planes) fetch(wn);
         __syncthreads();
         fft_smem<N, +1, T>(buf, t, a.tw);
@@ -407,7 +412,7 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
     for (int q = 0; q < Q; q++) {
         const int x = t + q * T;
         const float amp = a.phase ? a.ws.amp[prow + x] * a.scale : a.scale;
-        a.image[prow + x] = make_float2(sr[q] * amp, si[q] * amp);
+        image[prow + x] = make_float2(sr[q] * amp, si[q] * amp);
     }
 }
 
@@ -424,6 +429,10 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
     float *wal = wah + N, *wbh = wal + N, *wbl = wbh + N;
     const int y = blockIdx.x, t = threadIdx.x;
     const size_t prow = (size_t)y * N;
+    const size_t jp = (size_t)blockIdx.y * a.planes;
+    float2 *gridj = a.grid + jp * a.ny * N;
+    const unsigned char *plane_need = a.m.plane_need + jp;
+    const float2 *image = a.image + (size_t)blockIdx.y * a.ny * N;
     if (a.phase) {
         for (int x = t; x < N; x += T) {
             wah[x] = a.ws.ah[prow + x];
@@ -433,18 +442,18 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
         }
     }
     unsigned char *smask = reinterpret_cast<unsigned char *>(wbl + N);   // [planes][ntu]
-    for (int i = t; i < a.planes * a.ntu; i += T) smask[i] = a.m.need_col[i];
+    for (int i = t; i < a.planes * a.ntu; i += T) smask[i] = a.m.need_col[jp * a.ntu + i];
     float2 im[Q];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         const int x = t + q * T;
-        const float2 v = a.image[prow + x];
+        const float2 v = image[prow + x];
         float amp = a.phase ? a.ws.amp[prow + x] * a.scale : a.scale;
         if (!(amp == amp)) amp = 0.f;   // pixels where the forward is NaN are excluded
         im[q] = make_float2(v.x * amp, v.y * amp);
     }
     for (int w = 0; w < a.planes; w++) {
-        if (!a.m.plane_need[w]) continue;
+        if (!plane_need[w]) continue;
         __syncthreads();
         const float wf = (float)w;
 #pragma unroll
@@ -461,7 +470,7 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
         }
         __syncthreads();
         fft_smem<N, -1, T>(buf, t, a.tw);
-        float2 *dst = a.grid + ((size_t)w * a.ny + y) * N;
+        float2 *dst = gridj + ((size_t)w * a.ny + y) * N;
         for (int x = t; x < N; x += T)
             if (smask[w * a.ntu + (x >> a.tsh)]) __stcg(dst + x, buf[pidx(x)]);
     }
@@ -554,7 +563,7 @@ cudaError_t run_cols(const ColArgs &a, int planes, cudaStream_t s)
     return cudaGetLastError();
 }
 
-template <int N> cudaError_t run_rows_wc(const RowArgs &a, bool adjoint, cudaStream_t s)
+template <int N> cudaError_t run_rows_wc(const RowArgs &a, int jobs, bool adjoint, cudaStream_t s)
 {
     const size_t smem = row_smem<N>(a.planes, a.ntu);
     const void *k = adjoint ? (const void *)k_rows_wc_adj<N> : (const void *)k_rows_wc<N>;
@@ -562,7 +571,7 @@ template <int N> cudaError_t run_rows_wc(const RowArgs &a, bool adjoint, cudaStr
     if (e != cudaSuccess) return e;
     RowArgs ra = a;
     void *args[] = {&ra};
-    return cudaLaunchKernel(k, dim3(a.ny), dim3(fft_threads<N>()), args, smem, s);
+    return cudaLaunchKernel(k, dim3(a.ny, jobs), dim3(fft_threads<N>()), args, smem, s);
 }
 
 template <int N, int S> cudaError_t run_rows_plain(float2 *grid, const float2 *tw, int ny,
@@ -596,10 +605,10 @@ template <int S, int MODE> cudaError_t cols_dispatch(int n, const ColArgs &a, in
     return cudaErrorInvalidValue;
 }
 
-cudaError_t rows_wc_dispatch(int n, const RowArgs &a, bool adjoint, cudaStream_t s)
+cudaError_t rows_wc_dispatch(int n, const RowArgs &a, int jobs, bool adjoint, cudaStream_t s)
 {
     switch (n) {
-#define WSG_C(NN) case NN: return run_rows_wc<NN>(a, adjoint, s);
+#define WSG_C(NN) case NN: return run_rows_wc<NN>(a, jobs, adjoint, s);
         WSG_FFT_SIZES(WSG_C)
 #undef WSG_C
     }
@@ -650,18 +659,18 @@ cudaError_t launch_image_fwd_fused(const GeomParams &g, float2 *grid, float2 *im
     ColArgs c{grid, twy, g.nx, g.ny, g.tile, g.ntu, g.ntv, tile_shift(g.tile), m};
     cudaError_t e = cols_dispatch<+1, kColsFwd>(g.ny, c, g.planes, s);
     if (e != cudaSuccess) return e;
-    RowArgs r{grid, image, twx, g.nx, g.ny, g.planes, g.tile, g.ntu, phase ? 1 : 0,
+    RowArgs r{grid, image, twx, g.nx, g.ny, g.wplanes, g.tile, g.ntu, phase ? 1 : 0,
               tile_shift(g.tile), ws, (float)scale, m};
-    return rows_wc_dispatch(g.nx, r, false, s);
+    return rows_wc_dispatch(g.nx, r, g.planes / g.wplanes, false, s);
 }
 
 cudaError_t launch_image_adj_fused(const GeomParams &g, const float2 *image, float2 *grid,
                                    const float2 *twx, const float2 *twy, const WScreen &ws,
                                    const FftMasks &m, bool phase, double scale, cudaStream_t s)
 {
-    RowArgs r{grid, const_cast<float2 *>(image), twx, g.nx, g.ny, g.planes, g.tile, g.ntu,
+    RowArgs r{grid, const_cast<float2 *>(image), twx, g.nx, g.ny, g.wplanes, g.tile, g.ntu,
               phase ? 1 : 0, tile_shift(g.tile), ws, (float)scale, m};
-    cudaError_t e = rows_wc_dispatch(g.nx, r, true, s);
+    cudaError_t e = rows_wc_dispatch(g.nx, r, g.planes / g.wplanes, true, s);
     if (e != cudaSuccess) return e;
     ColArgs c{grid, twy, g.nx, g.ny, g.tile, g.ntu, g.ntv, tile_shift(g.tile), m};
     return cols_dispatch<-1, kColsAdj>(g.ny, c, g.planes, s);

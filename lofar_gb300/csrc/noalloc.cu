@@ -134,6 +134,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     g.nx = grid_size_x;
     g.ny = grid_size_y;
     g.planes = num_w_planes;
+    g.wplanes = num_w_planes;
     g.half = (w_support - 1) / 2;
     g.tile = kNoAllocTile;
     g.ntu = (grid_size_x + kNoAllocTile - 1) / kNoAllocTile;

@@ -1,17 +1,22 @@
 // Internal declarations shared by the translation units of libwstack_gb300.so.
 //
-// Data layout in HBM (one plan, P planes of Ny x Nx cells, tile edge T):
-//   grid      [P][Ny][Nx] complex (float2 for FP32C, double2 for FP64),
-//             the reference's [w][v][u][re,im] layout (w-stacking.cu:90)
-//   bins      (plane, tile-row, tile-col) in row-major order,
-//             bin = (w*ntv + tv)*ntu + tu; per-bin record counts, offsets
+// Data layout in HBM (one plan: J jobs of P planes of Ny x Nx cells, tile
+// edge T; a single image is J = 1, a (channel, polarisation) batch has one
+// job per pair, stacked along the plane axis):
+//   grid      [J*P][Ny][Nx] complex (float2 for FP32C, double2 for FP64),
+//             per job the reference's [w][v][u][re,im] layout
+//             (w-stacking.cu:90); cube plane = job*P + w
+//   bins      (cube plane, tile-row, tile-col) in row-major order,
+//             bin = (plane*ntv + tv)*ntu + tu; per-bin record counts, offsets
 //   records   structure-of-arrays, grouped by bin, primaries first:
 //             rec_cell  u32   (cu + 32768) | (cv + 32768) << 16, the
 //                             measurement's cell relative to the tile origin
 //             rec_frac  float2/double2   pos - cell (exact in FP64)
 //             rec_val   float2/double2   sum_{f,p} weight*vis (the fold of
 //                             w-stacking.cu:98-112)
-//             rec_idx   u32   original measurement index
+//             rec_idx   u32   original measurement index (batch: index
+//                             of the visibility in the concatenated
+//                             [channel][measurement][pol] layout)
 //   A measurement whose support window touches k tiles has k records
 //   (halo duplication, k <= 4); the record in the tile holding its own
 //   (clamped) cell is its primary.
@@ -49,7 +54,8 @@ struct DevCounters {
 
 // Geometry of the coordinate step (w-stacking.cu:66-77) and the tiling.
 struct GeomParams {
-    int nx, ny, planes, half, tile, ntu, ntv;
+    int nx, ny, planes, half, tile, ntu, ntv;   // planes: all jobs' planes
+    int wplanes;                                // w-planes of one job
     int u_pow2, w_pow2;   // dx (dw) is an exact power of two: 1/dx == 2^ku
     int ku, kw;
     double dx, dw;
@@ -147,6 +153,27 @@ cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu,
                                const float *vi, const float *wt, long long n, long long nf,
                                long long np, const BinBuffers &b, const RecBuffers &r,
                                cudaStream_t s);
+
+// One channel of a (channel, polarisation) batch: its measurements are
+// global indices [m0, m0 + n) of the concatenated batch; its visibilities
+// start at vis0 in the concatenated [channel][measurement][pol] layout.
+struct ChanDesc {
+    const double *uu, *vv, *ww;
+    const float *vr, *vi, *wt;   // [n][pols]
+    long long m0, n;
+    unsigned long long vis0;
+};
+constexpr int kMaxChannels = 2048;
+struct ChanTable {
+    const ChanDesc *ch;           // device array [nch]
+    const long long *m0;          // device array [nch]: ch[c].m0
+    int nch, pols;
+    long long ntot;               // sum of n
+};
+cudaError_t launch_bin_count_batch(const GeomParams &g, const ChanTable &t, const BinBuffers &b,
+                                   cudaStream_t s);
+cudaError_t launch_bin_scatter_batch(const GeomParams &g, int prec, const ChanTable &t,
+                                     const BinBuffers &b, const RecBuffers &r, cudaStream_t s);
 
 // ---- launchers (grid.cu) ----
 // partials: FP32C partial tiles of split bins (max_slots * tile^2 float2),

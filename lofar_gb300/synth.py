@@ -184,6 +184,89 @@ def observe(*, n_stations: int, diameter_m: float, hours: float, n_vis: int,
                   seeds=(station_seed, sky_seed, noise_seed)))
 
 
+# Polarisation responses of the batch generator: XX, XY, YX, YY of a weakly
+# polarised sky (Stokes Q = 0.05 I, U + iV leakage 0.05 at 0.3 rad);
+# fewer polarisations take XX (and YY).
+POL_GAINS = {1: (1.0,), 2: (1.0, 0.9),
+             4: (1.0, 0.05 * np.exp(0.3j), 0.05 * np.exp(-0.3j), 0.9)}
+
+
+@dataclass
+class BatchObservation:
+    """Per-channel inputs of a (channel, polarisation) batch.
+
+    channels[c] = (uu, vv, ww, vis_real, vis_img, weight): uvw float64 [n_c]
+    normalised on one grid shared by all channels (uvw in wavelengths scale
+    with frequency), values and weights float32 [n_c][pols].
+    """
+    channels: list
+    pols: int
+    freqs: np.ndarray
+    flag_fraction: np.ndarray
+    uvmin: float
+    uvmax: float
+    wmin: float
+    wmax: float
+
+    @property
+    def resolution(self) -> float:
+        return reference_resolution(self.uvmin, self.uvmax)
+
+    @property
+    def n_vis(self) -> int:
+        return sum(int(ch[0].shape[0]) for ch in self.channels) * self.pols
+
+
+def observe_batch(*, n_channels: int = 16, f_lo: float = 120e6, f_hi: float = 180e6,
+                  pols: int = 4, n_per_channel: int = 8_000_000, flag_max: float = 0.6,
+                  n_stations: int = 62, diameter_m: float = 8000.0, hours: float = 8.0,
+                  dec_deg: float = 45.0, station_seed: int = 1, sky_seed: int = 2,
+                  noise_seed: int = 3, flag_seed: int = 4, noise_sigma: float = 0.1,
+                  backend: str = "numpy", device: str = "cuda") -> BatchObservation:
+    """Channels uniform in [f_lo, f_hi]; each starts from the same n_per_channel
+    time-major measurements and drops a fraction U(0, flag_max) of them
+    (per channel, each measurement independently, seeded).  Every polarisation
+    of a channel carries the sky times its POL_GAINS entry plus its own noise."""
+    if pols not in POL_GAINS:
+        raise ValueError(f"pols must be one of {sorted(POL_GAINS)}")
+    bl = baselines_xyz(stations(n_stations, diameter_m, station_seed))
+    n_dumps = -(-n_per_channel // bl.shape[0])
+    um, vm, wm = (x.reshape(-1)[:n_per_channel] for x in
+                  uvw_tracks(bl, n_dumps, hours, dec_deg, C_LIGHT))   # metres
+    freqs = np.linspace(f_lo, f_hi, n_channels)
+    s_lo, s_hi = f_lo / C_LIGHT, f_hi / C_LIGHT
+    big_u = float(max(np.abs(um).max(), np.abs(vm).max())) * s_hi
+    lo_w, hi_w = float(wm.min()), float(wm.max())
+    wmin = lo_w * (s_hi if lo_w < 0 else s_lo)
+    wmax = hi_w * (s_hi if hi_w > 0 else s_lo)
+    frng = np.random.default_rng(flag_seed)
+    frac = frng.uniform(0.0, flag_max, n_channels)
+    sky = sky_model(sky_seed)
+    gains = np.asarray(POL_GAINS[pols], np.complex128)
+    chans = []
+    for c in range(n_channels):
+        keep = frng.random(n_per_channel) >= frac[c]
+        sc = freqs[c] / C_LIGHT
+        u, v, w = um[keep] * sc, vm[keep] * sc, wm[keep] * sc
+        if backend == "torch":
+            base = point_source_vis_torch(u, v, w, sky, device=device)
+        else:
+            base = point_source_vis(u, v, w, sky)
+        n = u.shape[0]
+        nrng = np.random.default_rng((noise_seed, c))
+        vis = base[:, None] * gains[None, :] + noise_sigma * (
+            nrng.standard_normal((n, pols)) + 1j * nrng.standard_normal((n, pols)))
+        chans.append((
+            np.ascontiguousarray(_below_one(0.5 + u / (2.0 * big_u))),
+            np.ascontiguousarray(_below_one(0.5 + v / (2.0 * big_u))),
+            np.ascontiguousarray(_below_one((w - wmin) / (wmax - wmin))),
+            np.ascontiguousarray(vis.real.astype(np.float32).reshape(-1)),
+            np.ascontiguousarray(vis.imag.astype(np.float32).reshape(-1)),
+            np.ones(n * pols, np.float32)))
+    return BatchObservation(channels=chans, pols=pols, freqs=freqs, flag_fraction=frac,
+                            uvmin=-big_u, uvmax=big_u, wmin=wmin, wmax=wmax)
+
+
 # Workload definitions (grid, planes, support, visibility generator).
 CONFIGS = {
     # plain FP64 w-stacking, runnable on the reference's OpenMP CPU path
@@ -195,6 +278,10 @@ CONFIGS = {
     # differentiation
     "c3": dict(nx=2048, ny=2048, planes=16, support=7,
                gen=dict(n_stations=62, diameter_m=8000.0, hours=8.0, n_vis=10_000_000)),
+    # batching: 16 channels x 4 polarisations, one grid each
+    "c4": dict(nx=2048, ny=2048, planes=16, support=7,
+               gen=dict(n_channels=16, f_lo=120e6, f_hi=180e6, pols=4, n_per_channel=8_000_000,
+                        flag_max=0.6, n_stations=62, diameter_m=8000.0, hours=8.0)),
     # large single image
     "c5": dict(nx=8192, ny=8192, planes=128, support=9,
                gen=dict(n_stations=62, diameter_m=8000.0, hours=12.0, n_vis=400_000_000)),

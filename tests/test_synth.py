@@ -40,3 +40,28 @@ def test_point_source_visibility_model():
 
 def test_reference_resolution_rule():
     assert synth.reference_resolution(-1499.9, 1428.6) == 1.0 / 1499
+
+
+def test_batch_generator_is_seeded_and_shares_one_grid():
+    a = synth.observe_batch(n_channels=4, pols=4, n_per_channel=3000, n_stations=20,
+                            diameter_m=2000.0, hours=2.0)
+    b = synth.observe_batch(n_channels=4, pols=4, n_per_channel=3000, n_stations=20,
+                            diameter_m=2000.0, hours=2.0)
+    assert len(a.channels) == 4
+    for ca, cb in zip(a.channels, b.channels):
+        for x, y in zip(ca, cb):
+            assert np.array_equal(x, y)
+    counts = [c[0].shape[0] for c in a.channels]
+    # per-channel flagging: uneven counts, each between 40% and 100% of 3000
+    assert len(set(counts)) == 4 and all(0.35 * 3000 < n <= 3000 for n in counts)
+    for c in a.channels:
+        n = c[0].shape[0]
+        assert all(x.shape == (n,) for x in c[:3])
+        assert all(x.shape == (n * 4,) and x.dtype == np.float32 for x in c[3:])
+        for x in c[:3]:
+            assert x.min() >= 0.0 and x.max() < 1.0
+    # uv extent grows with frequency on the shared grid
+    spread = [np.abs(c[0] - 0.5).max() for c in a.channels]
+    assert spread == sorted(spread)
+    assert a.n_vis == sum(counts) * 4
+    assert 0.0 <= a.flag_fraction.min() and a.flag_fraction.max() <= 0.6
