@@ -51,21 +51,32 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
-                    help="c2: one 4096^2 x 32 image (default); c4: the channel x pol batch")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
+                    help="c2: one 4096^2 x 32 image (default); c4: the channel x pol batch; "
+                         "c5: one 8192^2 x 128 image, support 9, 400M visibilities")
+    ap.add_argument("--subset", type=int, default=1_000_000,
+                    help="c5: visibilities in the subset checked against the FP64 oracle")
+    ap.add_argument("--window", type=int, default=512, help="c5: edge of the checked window")
     ap.add_argument("--per-channel", type=int, default=8_000_000,
                     help="c4: measurements per channel before flagging")
     ap.add_argument("--channels", type=int, default=16)
-    ap.add_argument("--nvis", type=int, default=50_000_000)
-    ap.add_argument("--nx", type=int, default=4096)
-    ap.add_argument("--planes", type=int, default=32)
-    ap.add_argument("--support", type=int, default=7)
+    ap.add_argument("--nvis", type=int, default=None, help="default: the workload's")
+    ap.add_argument("--nx", type=int, default=None)
+    ap.add_argument("--planes", type=int, default=None)
+    ap.add_argument("--support", type=int, default=None)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
-    return ap.parse_args()
+    a = ap.parse_args()
+    from lofar_gb300 import synth
+    cfg = synth.CONFIGS["c5" if a.workload == "c5" else "c2"]
+    a.nvis = cfg["gen"]["n_vis"] if a.nvis is None else a.nvis
+    a.nx = cfg["nx"] if a.nx is None else a.nx
+    a.planes = cfg["planes"] if a.planes is None else a.planes
+    a.support = cfg["support"] if a.support is None else a.support
+    return a
 
 
 def peaks():
@@ -642,6 +653,104 @@ def bench_batch(args, rank, world, peak, peak_kind):
     }
 
 
+# ---------------------------------------------------------------------------
+# the large single image, validated on a window and a subset
+# ---------------------------------------------------------------------------
+
+def bench_large(args, rank, world, peak, peak_kind):
+    """8192^2 x 128 planes (complex64, 69 GB), support 9, 400M visibilities:
+    FP32C forward + adjoint timed like the default workload; then a random
+    subset's forward image on a window, and the adjoint of an image supported
+    on that window, against the FP64 oracle's windowed forms."""
+    import torch
+    from lofar_gb300 import Plan, synth
+    from oracle import oracle as O
+
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    gen = dict(synth.CONFIGS["c5"]["gen"])
+    gen["n_vis"] = args.nvis
+    t0 = time.time()
+    d = synth.observe_device(device="cuda", **gen)
+    gen_s = time.time() - t0
+    ins = tuple(d[k] for k in ("uu", "vv", "ww", "vis_real", "vis_img", "weight"))
+    n, nx, P, S = d["n"], args.nx, args.planes, args.support
+    plan = Plan(nx, nx, P, S, precision="fp32c")
+    plan.set_wcorrection(d["resolution"], d["wmin"], d["wmax"])
+    plan.reserve(n)
+    image = torch.empty((nx, nx), dtype=torch.complex64, device="cuda")
+    out = torch.empty(n, dtype=torch.complex64, device="cuda")
+    run_plan_steps(plan, ins, image, out, args.warmup, False)
+    stats = plan.stats()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    total_ms, per = run_plan_steps(plan, ins, image, out, args.steps, True)
+    clk = clocks.stop()
+    ms = max_over_ranks(total_ms, world) / args.steps
+    stages = roofline(per, n, nx, P, 8, peak, peak_kind)
+    if rank != 0:
+        return None
+    del out
+    torch.cuda.empty_cache()
+
+    # validation: subset x window against the FP64 oracle
+    m_sub = min(n, args.subset)
+    rng = np.random.default_rng(11)
+    sel = torch.as_tensor(np.sort(rng.choice(n, m_sub, replace=False)), device="cuda")
+    sub = [x.index_select(0, sel).contiguous() for x in ins]
+    host = [x.cpu().numpy() for x in sub]
+    wn = min(args.window, nx // 2)
+    x0 = y0 = nx // 2        # pixel coordinate 0 (phase_correction.cu:164-169): finite r^2
+    kw = dict(num_w_planes=P, dx=1 / nx, dw=1 / P, w_support=S, nx=nx, ny=nx,
+              resolution=d["resolution"], wmin=d["wmin"], wmax=d["wmax"])
+    img = plan.image_forward(*sub)
+    win = img[y0:y0 + wn, x0:x0 + wn].cpu().numpy().astype(np.complex128)
+    t0 = time.time()
+    re, im = O.image_window(*host, x0=x0, y0=y0, wx=wn, wy=wn, **kw)
+    t_fwd = time.time() - t0
+    ref = re + 1j * im
+    fin = np.isfinite(ref)
+    fwd_rms = float(np.sqrt(np.mean(np.abs(win[fin] - ref[fin]) ** 2) / np.mean(np.abs(ref[fin]) ** 2)))
+    fwd_max = float(np.abs(win[fin] - ref[fin]).max() / np.abs(ref[fin]).max())
+    yw = rng.standard_normal((wn, wn)) + 1j * rng.standard_normal((wn, wn))
+    full = torch.zeros((nx, nx), dtype=torch.complex64, device="cuda")
+    full[y0:y0 + wn, x0:x0 + wn] = torch.as_tensor(yw.astype(np.complex64), device="cuda")
+    g = plan.image_adjoint(full).cpu().numpy().astype(np.complex128)
+    t0 = time.time()
+    a = O.adjoint_window(yw.real, yw.imag, host[0], host[1], host[2], x0=x0, y0=y0, **kw)
+    t_adj = time.time() - t0
+    aref = a[:, 0] + 1j * a[:, 1]
+    adj_rms = float(np.sqrt(np.mean(np.abs(g - aref) ** 2) / np.mean(np.abs(aref) ** 2)))
+    g_ = stages["gridding(bin+grid)"]
+    return {
+        "metric": METRIC, "value": whole_job_mvis(n, world, ms), "unit": "Mvis/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32c",
+        "data": "synthetic (seeded; 62 stations, 8 km, 12 h, 20 point sources + noise; "
+                "generated on the device)",
+        "config": {"workload": f"large single image: {nx}x{nx} grid, {P} w-planes "
+                               f"(complex64, {P * nx * nx * 8 / 1e9:.1f} GB), support {S}, "
+                               f"{n} visibilities",
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
+        "roofline": {"bound": "hbm", "kernel": "gridding stage (bin_count+bin_scan+bin_scatter+grid)",
+                     "achieved": g_["gbs"], "peak": peak, "unit": "GB/s", "frac": g_["frac"],
+                     "peak_source": f"{peak_kind} hbm copy bandwidth",
+                     "traffic": None, "algorithmic_bytes_per_launch": g_["bytes"]},
+        "stages": stages,
+        "validation": {"subset": m_sub, "window": [x0, y0, wn, wn],
+                       "forward_window_rel_rms": fwd_rms, "forward_window_rel_max": fwd_max,
+                       "forward_window_finite": int(fin.sum()),
+                       "adjoint_subset_rel_rms": adj_rms,
+                       "oracle_seconds": {"forward": t_fwd, "adjoint": t_adj},
+                       "oracle": "FP64 windowed forms of the oracle (per-plane gridding, "
+                                 "row FFT, DFT to the window, w-correction)"},
+        "gpu_launches": args.steps * sum(OUR_KERNELS_PER_STEP.values()),
+        "clocks": clk, "binning": stats, "plan_device_bytes": plan.device_bytes(),
+        "gen_s": gen_s,
+    }
+
+
 def roofline(per, n, nx, P, sc, peak, peak_kind):
     ab = algorithmic_bytes(n, nx, nx, P, sc)
     med = {s: statistics.median(v) for s, v in per.items() if v}
@@ -676,8 +785,9 @@ def main():
 
     import torch
     peak, peak_kind = peaks()
-    if args.workload == "c4":
-        line = bench_batch(args, rank, world, peak, peak_kind)
+    if args.workload in ("c4", "c5"):
+        fn = bench_batch if args.workload == "c4" else bench_large
+        line = fn(args, rank, world, peak, peak_kind)
         if line is not None:
             print(json.dumps(line))
         return 0

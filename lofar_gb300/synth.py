@@ -184,6 +184,67 @@ def observe(*, n_stations: int, diameter_m: float, hours: float, n_vis: int,
                   seeds=(station_seed, sky_seed, noise_seed)))
 
 
+def observe_device(*, n_stations: int, diameter_m: float, hours: float, n_vis: int,
+                   freq_hz: float = 150e6, dec_deg: float = 45.0, station_seed: int = 1,
+                   sky_seed: int = 2, noise_seed: int = 3, noise_sigma: float = 0.1,
+                   device: str = "cuda", chunk_dumps: int = 2048) -> dict:
+    """observe() for workloads too large for host memory: the same stations,
+    tracks, sky and normalisation, generated dump-chunk by dump-chunk straight
+    into device tensors (uu, vv, ww float64; vis_real, vis_img, weight float32).
+    The noise comes from a seeded torch generator on the device, so its values
+    differ from observe()'s.  Returns a dict with the tensors and the metadata
+    (wmin, wmax, uvmin, uvmax, resolution)."""
+    import torch
+    bl = baselines_xyz(stations(n_stations, diameter_m, station_seed))
+    n_bl = bl.shape[0]
+    n_dumps = -(-n_vis // n_bl)
+    hours_all = np.linspace(-hours / 2, hours / 2, n_dumps)
+
+    def tracks(d0, d1):
+        h = np.deg2rad(hours_all[d0:d1] * 15.0)[:, None]
+        d = math.radians(dec_deg)
+        lx, ly, lz = bl[None, :, 0], bl[None, :, 1], bl[None, :, 2]
+        sh, ch = np.sin(h), np.cos(h)
+        scale = freq_hz / C_LIGHT
+        u = (sh * lx + ch * ly) * scale
+        v = (-math.sin(d) * ch * lx + math.sin(d) * sh * ly + math.cos(d) * lz) * scale
+        w = (math.cos(d) * ch * lx - math.cos(d) * sh * ly + math.sin(d) * lz) * scale
+        rows = min((d1 - d0) * n_bl, n_vis - d0 * n_bl)
+        return (u.reshape(-1)[:rows], v.reshape(-1)[:rows], w.reshape(-1)[:rows])
+
+    big_u, wmin, wmax = 0.0, math.inf, -math.inf
+    umin, umax = math.inf, -math.inf
+    for d0 in range(0, n_dumps, chunk_dumps):
+        u, v, w = tracks(d0, min(d0 + chunk_dumps, n_dumps))
+        big_u = max(big_u, float(np.abs(u).max()), float(np.abs(v).max()))
+        wmin, wmax = min(wmin, float(w.min())), max(wmax, float(w.max()))
+        umin = min(umin, float(u.min()), float(v.min()))
+        umax = max(umax, float(u.max()), float(v.max()))
+    out = {k: torch.empty(n_vis, dtype=torch.float64, device=device) for k in ("uu", "vv", "ww")}
+    for k in ("vis_real", "vis_img"):
+        out[k] = torch.empty(n_vis, dtype=torch.float32, device=device)
+    out["weight"] = torch.ones(n_vis, dtype=torch.float32, device=device)
+    s, l, m, nn = (torch.as_tensor(x, dtype=torch.float64, device=device) for x in sky_model(sky_seed))
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(noise_seed))
+    below = float(np.nextafter(1.0, 0.0))
+    for d0 in range(0, n_dumps, chunk_dumps):
+        u, v, w = (torch.as_tensor(x, device=device) for x in tracks(d0, min(d0 + chunk_dumps, n_dumps)))
+        a, b = d0 * n_bl, d0 * n_bl + u.shape[0]
+        ph = -2.0 * math.pi * (u[:, None] * l + v[:, None] * m + w[:, None] * (nn - 1.0))
+        re = (s * torch.cos(ph)).sum(1) + noise_sigma * torch.randn(b - a, generator=gen, device=device, dtype=torch.float64)
+        im = (s * torch.sin(ph)).sum(1) + noise_sigma * torch.randn(b - a, generator=gen, device=device, dtype=torch.float64)
+        out["uu"][a:b] = torch.clamp_max(0.5 + u / (2.0 * big_u), below)
+        out["vv"][a:b] = torch.clamp_max(0.5 + v / (2.0 * big_u), below)
+        out["ww"][a:b] = torch.clamp_max((w - wmin) / (wmax - wmin), below)
+        out["vis_real"][a:b] = re.float()
+        out["vis_img"][a:b] = im.float()
+    out.update(wmin=wmin, wmax=wmax, uvmin=umin, uvmax=umax,
+               resolution=reference_resolution(umin, umax), n=n_vis, n_baselines=n_bl,
+               n_dumps=n_dumps)
+    return out
+
+
 # Polarisation responses of the batch generator: XX, XY, YX, YY of a weakly
 # polarised sky (Stokes Q = 0.05 I, U + iV leakage 0.05 at 0.3 rad);
 # fewer polarisations take XX (and YY).

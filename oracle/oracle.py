@@ -67,6 +67,17 @@ def load_oracle() -> ctypes.CDLL:
         lib.oracle_phase_adjoint.restype = None
         lib.oracle_resolution.argtypes = [ctypes.c_double, ctypes.c_double]
         lib.oracle_resolution.restype = ctypes.c_double
+        _i, _l, _d, _p = ctypes.c_int, ctypes.c_long, ctypes.c_double, ctypes.c_void_p
+        lib.oracle_grid_plane.argtypes = [_i, _i, _l, _l, _l, _c_double_p, _c_double_p,
+                                          _c_double_p, _c_float_p, _c_float_p, _c_float_p, _d,
+                                          _d, _i, _i, _i, _c_double_p, _p, _i]
+        lib.oracle_grid_plane.restype = None
+        lib.oracle_degrid_plane.argtypes = [_i, _i, _l, _c_double_p, _c_double_p, _c_double_p,
+                                            _d, _d, _i, _i, _i, _p, _p, _p, _i]
+        lib.oracle_degrid_plane.restype = None
+        lib.oracle_phase_window.argtypes = [_c_double_p, _c_double_p, _c_double_p, _i, _i, _i,
+                                            _i, _i, _i, _i, _i, _d, _d, _d, _i, _i]
+        lib.oracle_phase_window.restype = None
         _libs["oracle"] = lib
     return _libs["oracle"]
 
@@ -217,3 +228,107 @@ def image_adjoint(image_real, image_imag, uu, vv, ww, *, num_w_planes, dx, dw, w
     g = fft_planes_adjoint(planes)
     return degrid(uu, vv, ww, g, num_w_planes=num_w_planes, dx=dx, dw=dw, w_support=w_support,
                   nx=nx, ny=ny, num_threads=num_threads)
+
+
+
+def _ifft_rows(g, workers):
+    try:
+        import scipy.fft as sfft
+        return sfft.ifft(g, axis=1, workers=workers)
+    except ImportError:  # pragma: no cover
+        return np.fft.ifft(g, axis=1)
+
+
+def _fft_rows(g, workers):
+    try:
+        import scipy.fft as sfft
+        return sfft.fft(g, axis=1, workers=workers)
+    except ImportError:  # pragma: no cover
+        return np.fft.fft(g, axis=1)
+
+
+def image_window(uu, vv, ww, vis_real, vis_img, weight, *, num_w_planes, freq_per_chan=1,
+                 polarizations=1, dx, dw, w_support, nx, ny, resolution, wmin, wmax, x0, y0,
+                 wx, wy, num_threads=0):
+    """Pixels [y0, y0+wy) x [x0, x0+wx) of image_forward(...), one plane at a time
+    (no FP64 cube in memory): returns (image_real, image_imag) [wy][wx] float64.
+
+    Per plane: oracle_grid_plane (the reference's gridding arithmetic), then the
+    plane's inverse DFT on the window: an FFT along u of the rows that hold
+    taps (the FFTW_BACKWARD stand-in, as in fft_planes), a direct DFT along v
+    from those rows to the window's rows, the 1/(nx*ny) scale, and the
+    w-correction of the window's pixels (oracle_phase_window)."""
+    uu, vv, ww = _c(uu, np.float64), _c(vv, np.float64), _c(ww, np.float64)
+    vr, vi, wt = _c(vis_real, np.float32), _c(vis_img, np.float32), _c(weight, np.float32)
+    n = uu.shape[0]
+    L = load_oracle()
+    assert 0 <= x0 and x0 + wx <= nx and 0 <= y0 and y0 + wy <= ny
+    workers = num_threads if num_threads > 0 else -1
+    buf = np.zeros((ny, nx, 2), np.float64)
+    bufc = buf.view(np.complex128).reshape(ny, nx)
+    rows = np.zeros(ny, np.uint8)
+    re = np.zeros((wy, wx), np.float64)
+    im = np.zeros((wy, wx), np.float64)
+    ys = np.arange(y0, y0 + wy)
+    tw = np.exp(2j * np.pi * np.arange(ny) / ny)
+    for w in range(num_w_planes):
+        rows[:] = 0
+        L.oracle_grid_plane(w, num_w_planes, n, freq_per_chan, polarizations, _dp(uu), _dp(vv),
+                            _dp(ww), _fp(vr), _fp(vi), _fp(wt), dx, dw, w_support, nx, ny,
+                            _dp(buf), rows.ctypes.data, num_threads)
+        ks = np.nonzero(rows)[0]
+        if ks.size == 0:
+            continue
+        g = bufc[ks]
+        bufc[ks] = 0.0
+        r = _ifft_rows(g, workers)[:, x0:x0 + wx]            # includes 1/nx
+        ey = tw[np.outer(ys, ks) % ny]
+        plane = (ey @ r) / ny
+        pl = np.ascontiguousarray(np.stack([plane.real, plane.imag], -1))
+        L.oracle_phase_window(_dp(pl), _dp(re), _dp(im), w, num_w_planes, x0, y0, wx, wy, nx,
+                              ny, resolution, wmin, wmax, 0, num_threads)
+    return re, im
+
+
+def adjoint_window(image_real, image_imag, uu, vv, ww, *, x0, y0, num_w_planes, dx, dw,
+                   w_support, nx, ny, resolution, wmin, wmax, num_threads=0):
+    """image_adjoint(...) for an image that is zero outside the window whose
+    [wy][wx] values are given at offset (x0, y0): per-measurement [N][2].
+
+    Per plane: the w-correction adjoint on the window (oracle_phase_window),
+    the forward DFT scaled by 1/(nx*ny) evaluated on the grid rows the plane's
+    measurements read (a direct DFT along v, then an FFT along u), and
+    oracle_degrid_plane."""
+    re, im = _c(image_real, np.float64), _c(image_imag, np.float64)
+    wy, wx = re.shape
+    uu, vv, ww = _c(uu, np.float64), _c(vv, np.float64), _c(ww, np.float64)
+    n = uu.shape[0]
+    L = load_oracle()
+    assert 0 <= x0 and x0 + wx <= nx and 0 <= y0 and y0 + wy <= ny
+    workers = num_threads if num_threads > 0 else -1
+    buf = np.zeros((ny, nx, 2), np.float64)
+    bufc = buf.view(np.complex128).reshape(ny, nx)
+    rows = np.zeros(ny, np.uint8)
+    out = np.zeros((n, 2), np.float64)
+    pl = np.zeros((wy, wx, 2), np.float64)
+    ys = np.arange(y0, y0 + wy)
+    tw = np.exp(-2j * np.pi * np.arange(ny) / ny)
+    for w in range(num_w_planes):
+        rows[:] = 0
+        L.oracle_degrid_plane(w, num_w_planes, n, _dp(uu), _dp(vv), _dp(ww), dx, dw, w_support,
+                              nx, ny, None, None, rows.ctypes.data, num_threads)
+        ks = np.nonzero(rows)[0]
+        if ks.size == 0:
+            continue
+        L.oracle_phase_window(_dp(pl), _dp(re), _dp(im), w, num_w_planes, x0, y0, wx, wy, nx,
+                              ny, resolution, wmin, wmax, 1, num_threads)
+        p = pl[..., 0] + 1j * pl[..., 1]
+        ey = tw[np.outer(ks, ys) % ny]
+        t = np.zeros((ks.size, nx), np.complex128)
+        t[:, x0:x0 + wx] = ey @ p
+        bufc[ks] = _fft_rows(t, workers) / (float(nx) * float(ny))
+        L.oracle_degrid_plane(w, num_w_planes, n, _dp(uu), _dp(vv), _dp(ww), dx, dw, w_support,
+                              nx, ny, buf.ctypes.data, out.ctypes.data, rows.ctypes.data,
+                              num_threads)
+        bufc[ks] = 0.0
+    return out

@@ -18,6 +18,13 @@
  *                             the folded measurement value to the grid (the
  *                             reference has no adjoint)
  *   oracle_phase_adjoint      the exact adjoint of oracle_phase_correction
+ *   oracle_grid_plane,        oracle_wstack / oracle_degrid restricted to
+ *   oracle_degrid_plane       the measurements of one w-plane, on a single
+ *                             [Ny][Nx] plane buffer
+ *   oracle_phase_window       oracle_phase_correction (and its adjoint) for
+ *                             one plane on a window of pixels
+ * The last three let oracle.py evaluate a window of the image of grids whose
+ * FP64 cube does not fit in host memory, one plane at a time.
  *
  * Parity is pinned against the reference itself: oracle/Makefile compiles the
  * reference's w-stacking.cu and phase_correction.cu as C into oracle/_ref/,
@@ -291,4 +298,177 @@ double oracle_resolution(double uvmin, double uvmax)
     if (a < 0) a = -a;
     if (b < 0) b = -b;
     return 1.0 / (double)(a > b ? a : b);
+}
+
+
+/* ------------------------------------------------------------------------
+ * Per-plane and windowed forms, for grids whose FP64 cube does not fit in
+ * host memory (oracle.py composes them with the per-plane FFT).
+ * ---------------------------------------------------------------------- */
+
+/*
+ * oracle_wstack for the measurements of plane w only, into buf ([ny][nx][2],
+ * accumulated); rows[k] is set for every grid row that receives a tap.
+ */
+void oracle_grid_plane(int w, int num_w_planes, long num_points, long freq_per_chan,
+                       long polarizations, const double *uu, const double *vv,
+                       const double *ww, const float *vis_real, const float *vis_img,
+                       const float *weight, double dx, double dw, int w_support,
+                       int grid_size_x, int grid_size_y, double *buf, unsigned char *rows,
+                       int num_threads)
+{
+    const int half = (w_support - 1) / 2;
+    const double std22 = 0.5;
+    const double norm = std22 / ORACLE_PI;
+#ifdef _OPENMP
+    if (num_threads > 0) omp_set_num_threads(num_threads);
+#else
+    (void)num_threads;
+#endif
+#pragma omp parallel for schedule(static)
+    for (long m = 0; m < num_points; m++) {
+        const int cw = (int)(ww[m] / dw);
+        if (cw != w || cw < 0 || cw >= num_w_planes) continue;
+        const long vbase = m * freq_per_chan * polarizations;
+        const double pu = uu[m] / dx;
+        const double pv = vv[m] / dx;
+        const int cu = (int)pu;
+        const int cv = (int)pv;
+        const long j0 = (cu > half - 1) ? cu - half : 0;
+        const long j1 = (cu < grid_size_x - half) ? cu + half : grid_size_x - 1;
+        const long k0 = (cv > half - 1) ? cv - half : 0;
+        const long k1 = (cv < grid_size_y - half) ? cv + half : grid_size_y - 1;
+        for (long k = k0; k <= k1; k++) {
+            const double dist_v = (double)k + 0.5 - pv;
+#pragma omp atomic write
+            rows[k] = 1;
+            for (long j = j0; j <= j1; j++) {
+                const double dist_u = (double)j + 0.5 - pu;
+                const long cell = 2 * (j + k * (long)grid_size_x);
+                const double cwt = oracle_gauss(norm, std22, dist_u, dist_v);
+                double acc_re = 0.0, acc_im = 0.0;
+                long fine = vbase;
+                for (long f = 0; f < freq_per_chan; f++) {
+                    long iw = vbase / freq_per_chan;
+                    for (long p = 0; p < polarizations; p++) {
+                        if (!isnan(vis_real[fine])) {
+                            acc_re += weight[iw] * vis_real[fine] * cwt;
+                            acc_im += weight[iw] * vis_img[fine] * cwt;
+                        }
+                        fine++;
+                        iw++;
+                    }
+                }
+#pragma omp atomic
+                buf[cell] += acc_re;
+#pragma omp atomic
+                buf[cell + 1] += acc_im;
+            }
+        }
+    }
+}
+
+/*
+ * oracle_degrid for the measurements of plane w only, reading the single
+ * plane buf ([ny][nx][2]); out[m] ([num_points][2]) is written for those
+ * measurements and left alone for the others.  rows[k] is set for every row
+ * they read (so a caller can evaluate the plane on those rows only).
+ * With buf == NULL only rows is set.
+ */
+void oracle_degrid_plane(int w, int num_w_planes, long num_points, const double *uu,
+                         const double *vv, const double *ww, double dx, double dw,
+                         int w_support, int grid_size_x, int grid_size_y, const double *buf,
+                         double *out, unsigned char *rows, int num_threads)
+{
+    const int half = (w_support - 1) / 2;
+    const double std22 = 0.5;
+    const double norm = std22 / ORACLE_PI;
+#ifdef _OPENMP
+    if (num_threads > 0) omp_set_num_threads(num_threads);
+#else
+    (void)num_threads;
+#endif
+#pragma omp parallel for schedule(static)
+    for (long m = 0; m < num_points; m++) {
+        const int cw = (int)(ww[m] / dw);
+        if (cw != w || cw < 0 || cw >= num_w_planes) continue;
+        const double pu = uu[m] / dx;
+        const double pv = vv[m] / dx;
+        const int cu = (int)pu;
+        const int cv = (int)pv;
+        const long j0 = (cu > half - 1) ? cu - half : 0;
+        const long j1 = (cu < grid_size_x - half) ? cu + half : grid_size_x - 1;
+        const long k0 = (cv > half - 1) ? cv - half : 0;
+        const long k1 = (cv < grid_size_y - half) ? cv + half : grid_size_y - 1;
+        double sre = 0.0, sim = 0.0;
+        for (long k = k0; k <= k1; k++) {
+#pragma omp atomic write
+            rows[k] = 1;
+            if (!buf) continue;
+            const double dist_v = (double)k + 0.5 - pv;
+            for (long j = j0; j <= j1; j++) {
+                const double dist_u = (double)j + 0.5 - pu;
+                const double cwt = oracle_gauss(norm, std22, dist_u, dist_v);
+                sre += cwt * buf[2 * (j + k * (long)grid_size_x)];
+                sim += cwt * buf[2 * (j + k * (long)grid_size_x) + 1];
+            }
+        }
+        if (buf) {
+            out[2 * m] = sre;
+            out[2 * m + 1] = sim;
+        }
+    }
+}
+
+/*
+ * One plane of oracle_phase_correction (adjoint = 0: image += phase * plane,
+ * accumulated) or of oracle_phase_adjoint (adjoint = 1: plane = conj(phase) *
+ * image, overwritten) on the window [x0, x0+wx) x [y0, y0+wy) of an
+ * xaxistot x yaxistot image; plane and image are [wy][wx] (plane interleaved
+ * re,im; image as two arrays).
+ */
+void oracle_phase_window(double *plane, double *image_real, double *image_imag, int w,
+                         int num_w_planes, int x0, int y0, int wx, int wy, int xaxistot,
+                         int yaxistot, double resolution, double wmin, double wmax, int adjoint,
+                         int num_threads)
+{
+    const double dw = (wmax - wmin) / (double)num_w_planes;
+    const double dwnorm = dw / (wmax - wmin);
+    const double wterm = wmin + w * dw;
+#ifdef _OPENMP
+    if (num_threads > 0) omp_set_num_threads(num_threads);
+#else
+    (void)num_threads;
+#endif
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int jy = 0; jy < wy; jy++) {
+        for (int i = 0; i < wx; i++) {
+            const size_t pix = (size_t)jy * wx + i;
+            if (num_w_planes <= 1) {
+                if (adjoint) {
+                    plane[2 * pix] = image_real[pix];
+                    plane[2 * pix + 1] = image_imag[pix];
+                } else {
+                    image_real[pix] += plane[2 * pix];
+                    image_imag[pix] += plane[2 * pix + 1];
+                }
+                continue;
+            }
+            const double xs = oracle_pixel_sin(x0 + i, xaxistot, resolution);
+            const double ys = oracle_pixel_sin(y0 + jy, yaxistot, resolution);
+            const double r2 = (xs * xs + ys * ys);
+            const double pre = cos(2.0 * ORACLE_PI * wterm * (sqrt(1 - r2) - 1.0));
+            const double pim = sin(2.0 * ORACLE_PI * wterm * (sqrt(1 - r2) - 1.0));
+            if (adjoint) {
+                const double amp = dwnorm * sqrt(1 - r2);
+                const double xr = image_real[pix], xi = image_imag[pix];
+                plane[2 * pix] = (pre * xr + pim * xi) * amp;
+                plane[2 * pix + 1] = (pre * xi - pim * xr) * amp;
+            } else {
+                const double a = plane[2 * pix], b = plane[2 * pix + 1];
+                image_real[pix] += (a * pre - b * pim) * dwnorm * sqrt(1 - r2);
+                image_imag[pix] += (a * pim + b * pre) * dwnorm * sqrt(1 - r2);
+            }
+        }
+    }
 }

@@ -137,3 +137,29 @@ def test_oracle_adjoint_dot_product():
 def test_resolution_rule_truncates_like_c_int_abs():
     assert O.resolution(-1499.9, 1428.6) == 1.0 / 1499
     assert O.resolution(-3.7, 1500.2) == 1.0 / 1500
+
+
+@pytest.mark.parametrize("nx,ny,planes,win", [(64, 64, 4, (20, 8, 16, 12)),
+                                              (48, 40, 3, (30, 25, 18, 15)),
+                                              (32, 32, 1, (0, 0, 32, 32))])
+def test_window_oracle_equals_full_chain(nx, ny, planes, win):
+    """The plane-by-plane windowed forms (used where the FP64 cube does not fit
+    in memory) equal the full oracle chain on the window."""
+    from lofar_gb300 import synth
+    obs = synth.observe(n_stations=16, diameter_m=1500.0, hours=2.0, n_vis=3000, sky_seed=9)
+    x0, y0, wx, wy = win
+    kw = dict(num_w_planes=planes, dx=1 / nx, dw=1 / planes, w_support=7, nx=nx, ny=ny,
+              resolution=1 / 400.0, wmin=obs.wmin, wmax=obs.wmax)
+    re, im = O.image_forward(obs.uu, obs.vv, obs.ww, obs.vis_real, obs.vis_img, obs.weight, **kw)
+    wr, wi = O.image_window(obs.uu, obs.vv, obs.ww, obs.vis_real, obs.vis_img, obs.weight,
+                            x0=x0, y0=y0, wx=wx, wy=wy, **kw)
+    ref = re[y0:y0 + wy, x0:x0 + wx] + 1j * im[y0:y0 + wy, x0:x0 + wx]
+    assert np.abs(wr + 1j * wi - ref).max() <= 1e-13 * np.abs(ref).max()
+    rng = np.random.default_rng(1)
+    y = rng.standard_normal((wy, wx)) + 1j * rng.standard_normal((wy, wx))
+    full = np.zeros((ny, nx), np.complex128)
+    full[y0:y0 + wy, x0:x0 + wx] = y
+    a_ref = O.image_adjoint(full.real, full.imag, obs.uu, obs.vv, obs.ww, **{
+        k: v for k, v in kw.items()})
+    a = O.adjoint_window(y.real, y.imag, obs.uu, obs.vv, obs.ww, x0=x0, y0=y0, **kw)
+    assert np.abs(a - a_ref).max() <= 1e-13 * np.abs(a_ref).max()
