@@ -691,10 +691,12 @@ def bench_large(args, rank, world, peak, peak_kind):
     stages = roofline(per, n, nx, P, 8, peak, peak_kind)
     if rank != 0:
         return None
+    plan_bytes = plan.device_bytes()
     del out
     torch.cuda.empty_cache()
 
-    # validation: subset x window against the FP64 oracle
+    # validation on a random subset: FP32C and FP64 on the device over the
+    # whole image, and both against the FP64 oracle on a window
     m_sub = min(n, args.subset)
     rng = np.random.default_rng(11)
     sel = torch.as_tensor(np.sort(rng.choice(n, m_sub, replace=False)), device="cuda")
@@ -704,24 +706,56 @@ def bench_large(args, rank, world, peak, peak_kind):
     x0 = y0 = nx // 2        # pixel coordinate 0 (phase_correction.cu:164-169): finite r^2
     kw = dict(num_w_planes=P, dx=1 / nx, dw=1 / P, w_support=S, nx=nx, ny=nx,
               resolution=d["resolution"], wmin=d["wmin"], wmax=d["wmax"])
-    img = plan.image_forward(*sub)
-    win = img[y0:y0 + wn, x0:x0 + wn].cpu().numpy().astype(np.complex128)
+    yw = rng.standard_normal((wn, wn)) + 1j * rng.standard_normal((wn, wn))
+    imgs, adjs = {}, {}
+    _GRIDS.pop(id(plan), None)
+    plan.close()
+    del plan, image
+    for prec in ("fp32c", "fp64"):
+        torch.cuda.empty_cache()
+        p = Plan(nx, nx, P, S, precision=prec)
+        p.set_wcorrection(d["resolution"], d["wmin"], d["wmax"])
+        imgs[prec] = p.image_forward(*sub).to(torch.complex64 if prec == "fp32c" else torch.complex128)
+        full = torch.zeros((nx, nx), dtype=p.cdtype, device="cuda")
+        full[y0:y0 + wn, x0:x0 + wn] = torch.as_tensor(yw, device="cuda").to(p.cdtype)
+        adjs[prec] = p.image_adjoint(full).cpu().numpy().astype(np.complex128)
+        del full
+        p.close()
+    a64 = imgs["fp64"]
+    a32 = imgs["fp32c"].to(torch.complex128)
+    fin = torch.isfinite(a64.real)
+    rms = float(torch.sqrt((a64[fin].abs() ** 2).mean()))
+    glob = float(torch.sqrt(((a32 - a64)[fin].abs() ** 2).mean())) / rms
+    nan_equal = bool(torch.equal(fin, torch.isfinite(a32.real)))
+    win32 = a32[y0:y0 + wn, x0:x0 + wn].cpu().numpy()
+    win64 = a64[y0:y0 + wn, x0:x0 + wn].cpu().numpy()
+    del imgs, a32, a64
+    torch.cuda.empty_cache()
     t0 = time.time()
     re, im = O.image_window(*host, x0=x0, y0=y0, wx=wn, wy=wn, **kw)
     t_fwd = time.time() - t0
     ref = re + 1j * im
-    fin = np.isfinite(ref)
-    fwd_rms = float(np.sqrt(np.mean(np.abs(win[fin] - ref[fin]) ** 2) / np.mean(np.abs(ref[fin]) ** 2)))
-    fwd_max = float(np.abs(win[fin] - ref[fin]).max() / np.abs(ref[fin]).max())
-    yw = rng.standard_normal((wn, wn)) + 1j * rng.standard_normal((wn, wn))
-    full = torch.zeros((nx, nx), dtype=torch.complex64, device="cuda")
-    full[y0:y0 + wn, x0:x0 + wn] = torch.as_tensor(yw.astype(np.complex64), device="cuda")
-    g = plan.image_adjoint(full).cpu().numpy().astype(np.complex128)
     t0 = time.time()
     a = O.adjoint_window(yw.real, yw.imag, host[0], host[1], host[2], x0=x0, y0=y0, **kw)
     t_adj = time.time() - t0
     aref = a[:, 0] + 1j * a[:, 1]
-    adj_rms = float(np.sqrt(np.mean(np.abs(g - aref) ** 2) / np.mean(np.abs(aref) ** 2)))
+
+    def rel(x, r):
+        return float(np.sqrt(np.mean(np.abs(x - r) ** 2) / np.mean(np.abs(r) ** 2)))
+    win_err = float(np.sqrt(np.mean(np.abs(win32 - ref) ** 2)))
+    validation = {
+        "subset": m_sub, "window": [x0, y0, wn, wn],
+        "fp32c_vs_fp64_image_rel_rms": glob, "nan_mask_equal": nan_equal,
+        "fp64_window_vs_oracle_rel_rms": rel(win64, ref),
+        "fp32c_window_vs_oracle_rms_over_image_rms": win_err / rms,
+        "fp32c_window_vs_oracle_rel_rms": rel(win32, ref),
+        "window_rms_over_image_rms": float(np.sqrt(np.mean(np.abs(ref) ** 2))) / rms,
+        "fp64_adjoint_vs_oracle_rel_rms": rel(adjs["fp64"], aref),
+        "fp32c_adjoint_vs_oracle_rel_rms": rel(adjs["fp32c"], aref),
+        "oracle_seconds": {"forward": t_fwd, "adjoint": t_adj},
+        "oracle": "FP64 windowed forms of the oracle (per-plane gridding, row FFT, DFT to the "
+                  "window, w-correction; adjoint likewise)",
+    }
     g_ = stages["gridding(bin+grid)"]
     return {
         "metric": METRIC, "value": whole_job_mvis(n, world, ms), "unit": "Mvis/s",
@@ -738,15 +772,9 @@ def bench_large(args, rank, world, peak, peak_kind):
                      "peak_source": f"{peak_kind} hbm copy bandwidth",
                      "traffic": None, "algorithmic_bytes_per_launch": g_["bytes"]},
         "stages": stages,
-        "validation": {"subset": m_sub, "window": [x0, y0, wn, wn],
-                       "forward_window_rel_rms": fwd_rms, "forward_window_rel_max": fwd_max,
-                       "forward_window_finite": int(fin.sum()),
-                       "adjoint_subset_rel_rms": adj_rms,
-                       "oracle_seconds": {"forward": t_fwd, "adjoint": t_adj},
-                       "oracle": "FP64 windowed forms of the oracle (per-plane gridding, "
-                                 "row FFT, DFT to the window, w-correction)"},
+        "validation": validation,
         "gpu_launches": args.steps * sum(OUR_KERNELS_PER_STEP.values()),
-        "clocks": clk, "binning": stats, "plan_device_bytes": plan.device_bytes(),
+        "clocks": clk, "binning": stats, "plan_device_bytes": plan_bytes,
         "gen_s": gen_s,
     }
 
