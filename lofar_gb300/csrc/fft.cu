@@ -449,8 +449,15 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
         const int x = t + q * T;
         const float2 v = image[prow + x];
         float amp = a.phase ? a.ws.amp[prow + x] * a.scale : a.scale;
-        if (!(amp == amp)) amp = 0.f;   // pixels where the forward is NaN are excluded
-        im[q] = make_float2(v.x * amp, v.y * amp);
+        if (!(amp == amp)) {
+            // pixels where the forward is NaN are excluded: zero value (the
+            // image may hold NaN there) and a zero phase (their w-screen
+            // entries are NaN too)
+            im[q] = make_float2(0.f, 0.f);
+            if (a.phase) wah[x] = wal[x] = wbh[x] = wbl[x] = 0.f;
+        } else {
+            im[q] = make_float2(v.x * amp, v.y * amp);
+        }
     }
     for (int w = 0; w < a.planes; w++) {
         if (!plane_need[w]) continue;

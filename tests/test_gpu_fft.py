@@ -80,3 +80,24 @@ def test_fused_forward_matches_oracle_image(gpu):
     ok = np.isfinite(ref)
     assert np.array_equal(np.isfinite(z), ok)
     assert _rel_rms(z[ok], ref[ok]) <= 1e-5
+
+
+def test_fused_adjoint_excludes_nan_pixels(gpu):
+    """Pixels where the forward is NaN (r^2 > 1) are excluded from the adjoint:
+    their image value (NaN here: the forward image itself is fed back) and
+    their NaN w-screen phase must not reach the transforms."""
+    import torch
+    from lofar_gb300 import Plan, synth
+    obs = synth.observe(n_stations=24, diameter_m=2000.0, hours=2.0, n_vis=30_000)
+    nx, planes, res = 256, 8, 1.0 / 150.0
+    outs = {}
+    for prec in ("fp64", "fp32c"):
+        p = Plan(nx, nx, planes, 7, precision=prec)
+        p.set_wcorrection(res, obs.wmin, obs.wmax)
+        img = p.image_forward(obs.uu, obs.vv, obs.ww, obs.vis_real, obs.vis_img, obs.weight)
+        nan = torch.isnan(img.real)
+        assert 0 < int(nan.sum()) < nx * nx // 2
+        outs[prec] = p.image_adjoint(img).to(torch.complex128).cpu().numpy()
+        p.close()
+    assert np.isfinite(outs["fp32c"]).all() and np.isfinite(outs["fp64"]).all()
+    assert _rel_rms(outs["fp32c"], outs["fp64"]) <= 1e-5
