@@ -703,7 +703,10 @@ def bench_large(args, rank, world, peak, peak_kind):
     sub = [x.index_select(0, sel).contiguous() for x in ins]
     host = [x.cpu().numpy() for x in sub]
     wn = min(args.window, nx // 2)
-    x0 = y0 = nx // 2        # pixel coordinate 0 (phase_correction.cu:164-169): finite r^2
+    # finite w-correction (pixel coordinate (iu - N/2) mod N small,
+    # phase_correction.cu:164-169) and away from the grid's Nyquist pixel N/2,
+    # where the Gaussian kernel's response is ~5e-5
+    x0 = y0 = 13 * nx // 16 - wn // 2
     kw = dict(num_w_planes=P, dx=1 / nx, dw=1 / P, w_support=S, nx=nx, ny=nx,
               resolution=d["resolution"], wmin=d["wmin"], wmax=d["wmax"])
     yw = rng.standard_normal((wn, wn)) + 1j * rng.standard_normal((wn, wn))

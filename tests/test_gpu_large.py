@@ -3,8 +3,16 @@ oracle's windowed forms, at a size the oracle finishes in seconds.
 
 The full configuration (8192^2 x 128 planes, 400M visibilities) runs in
 `bench.py --workload c5`, validated the same way on a 1M-visibility subset and
-a 512^2 window.  Here: 8192^2 x 8 planes, 200k visibilities, a 256^2 window at
-pixel coordinate 0 (where the w-correction is finite).
+a 512^2 window.  Here: 8192^2 x 8 planes, 200k visibilities, a 256^2 window.
+
+Where the window goes: the reference's pixel coordinate (iu - N/2) mod N
+(phase_correction.cu:164-169) makes the w-correction finite only for small
+coordinates, i.e. pixels from N/2 up; pixel N/2 itself is the grid's Nyquist
+frequency, where the Gaussian kernel's response is e^{-pi^2/2} per axis
+(~5e-5 in 2D), so image values and adjoint outputs there are heavy
+cancellations that magnify any non-FP64 rounding ~1e4x.  The window sits at
+13/16 of the grid instead: finite (r^2 < 0.9 at this resolution) and at
+0.22 cycles/cell, where the kernel's response is ~0.2.
 
 Tolerances:
   FP64 window vs oracle           relative rms 1e-11 (pins the FP64 form)
@@ -35,6 +43,10 @@ def case(gpu):
     return obs
 
 
+def window_origin(n, w):
+    return 13 * n // 16 - w // 2
+
+
 def _rel_rms(a, b):
     return float(np.sqrt(np.mean(np.abs(a - b) ** 2) / np.mean(np.abs(b) ** 2)))
 
@@ -43,7 +55,7 @@ def test_large_image_window_and_adjoint(case):
     import torch
     from lofar_gb300 import Plan
     o = case
-    x0 = y0 = NX // 2
+    x0 = y0 = window_origin(NX, WIN)
     kw = dict(num_w_planes=PLANES, dx=1 / NX, dw=1 / PLANES, w_support=SUPPORT, nx=NX, ny=NX,
               resolution=o.resolution, wmin=o.wmin, wmax=o.wmax)
     re, im = O.image_window(o.uu, o.vv, o.ww, o.vis_real, o.vis_img, o.weight, x0=x0, y0=y0,
