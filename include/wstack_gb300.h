@@ -290,10 +290,10 @@ WSG_API long long wsg_batch_device_bytes(wsg_batch *batch);
  * `stream` (a cudaStream_t, NULL = legacy default stream).
  * Its scratch is a fixed 64 MiB static device array per GPU, held until the
  * process exits; a call needing more than
- *     256 + 24*nbins + 8*ceil(nbins/4096) + 32768 + 160*num_points bytes
- *     (+ alignment),
+ *     2560 + 32*nbins + 16*ceil(nbins/4096) + 161*num_points bytes
+ *     (alignment included),
  *     nbins = num_w_planes*ceil(grid_size_y/64)*ceil(grid_size_x/64),
- * fails with WSG_ERR_CAPACITY (about 400,000 measurements on a 4096x4096x32
+ * fails with WSG_ERR_CAPACITY (about 390,000 measurements on a 4096x4096x32
  * grid).  All calls share that array: calls whose GPU work may overlap race
  * and must be serialised by the caller.  The first call on a device looks up
  * the array's device address and may load the device code: make it before

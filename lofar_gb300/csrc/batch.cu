@@ -70,7 +70,7 @@ int batch_enqueue_forward(wsg_batch *B, void *images)
     wsg_plan *p = B->p;
     const BinBuffers b = p->binbufs();
     const RecBuffers r = p->recbufs();
-    WSG_CUDA(cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(p->geom.nbins), p->stream));
+    WSG_CUDA(cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(p->geom.nbins, b.nsub), p->stream));
     WSG_CUDA(cudaMemsetAsync(b.ctr, 0, sizeof(DevCounters), p->stream));
     WSG_CUDA(launch_bin_count_batch(p->geom, B->tab, b, p->stream));
     WSG_CUDA(launch_bin_scan(p->geom, b, p->stream));

@@ -109,6 +109,7 @@ int wsg::plan_configure(wsg_plan *p)
     g.ny = p->ny;
     g.half = p->half;
     g.tile = p->tile;
+    g.bank_pitch = f32c_tile_pitch(p->tile, p->half);
     g.ntu = (p->nx + p->tile - 1) / p->tile;
     g.ntv = (p->ny + p->tile - 1) / p->tile;
     g.wplanes = p->planes;
@@ -145,7 +146,8 @@ int wsg::ensure_records(wsg_plan *p, long long n)
     // a support window of <= tile cells touches at most 2x2 tiles
     const unsigned long long need = (unsigned long long)(n > 0 ? n : 1) * 4ull;
     if (need <= p->rec_cap) return WSG_OK;
-    WSG_CUDA(p->bins.ensure(bin_buffer_bytes(p->geom.nbins, max_split_items(need, p->split))));
+    WSG_CUDA(p->bins.ensure(bin_buffer_bytes(p->geom.nbins, max_split_items(need, p->split),
+                                             kSubMax)));
     if (p->prec == WSG_FP32C)
         WSG_CUDA(p->partials.ensure(max_slots(need, p->split) * (size_t)p->tile * p->tile *
                                     sizeof(float2)));
@@ -412,7 +414,7 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
         return set_error(WSG_ERR_ARG, "NULL input pointer");
     WSG_TRY(ensure_records(p, n));
     const BinBuffers b = p->binbufs();
-    WSG_CUDA(cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(p->geom.nbins), p->stream));
+    WSG_CUDA(cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(p->geom.nbins, b.nsub), p->stream));
     WSG_CUDA(cudaMemsetAsync(b.ctr, 0, sizeof(DevCounters), p->stream));
     WSG_CUDA(launch_bin_count(p->geom, uu, vv, ww, n, b, p->stream));
     WSG_CUDA(launch_bin_scan(p->geom, b, p->stream));

@@ -11,12 +11,13 @@
 // allocating it.
 //
 // The array is a fixed 64 MiB of device memory per GPU that loads the library,
-// held until the process exits.  A call needs
-//     256 + 24*nbins + 8*ceil(nbins/4096) + 32768 + 160*num_points   bytes
-//     (plus 256-byte alignment padding),
+// held until the process exits.  A call needs at most
+//     2560 + 32*nbins + 16*ceil(nbins/4096) + 161*num_points   bytes
+//     (alignment padding included),
 //     nbins = num_w_planes * ceil(grid_size_y/64) * ceil(grid_size_x/64),
 // and is rejected with WSG_ERR_CAPACITY when that exceeds the array: for a
-// 4096x4096x32 grid that is about 400,000 measurements per call.
+// 4096x4096x32 grid that is about 390,000 measurements per call.  Its bin
+// table keeps one counter per bin and kind (no sub-ranges).
 //
 // All calls share the array and it keeps what the last call left in it; each
 // call clears the counters it needs before using them.  Calls whose GPU work
@@ -137,6 +138,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     g.wplanes = num_w_planes;
     g.half = (w_support - 1) / 2;
     g.tile = kNoAllocTile;
+    g.bank_pitch = f32c_tile_pitch(kNoAllocTile, g.half);
     g.ntu = (grid_size_x + kNoAllocTile - 1) / kNoAllocTile;
     g.ntv = (grid_size_y + kNoAllocTile - 1) / kNoAllocTile;
     g.nbins = (long long)num_w_planes * g.ntv * g.ntu;
@@ -151,14 +153,14 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     // scratch layout: counters | bin table | record cells | indices | fracs | values
     const unsigned long long cap = 4ull * (unsigned long long)(num_points > 0 ? num_points : 1);
     const size_t o_bins = up256(sizeof(DevCounters));
-    const size_t o_cell = o_bins + up256(bin_buffer_bytes(g.nbins, max_split_items(cap, kDefaultSplit)));
+    const size_t o_cell = o_bins + up256(bin_buffer_bytes(g.nbins, max_split_items(cap, kDefaultSplit), 1));
     const size_t o_idx = o_cell + up256(cap * sizeof(unsigned));
     const size_t o_frac = o_idx + up256(cap * sizeof(unsigned));
     const size_t o_val = o_frac + up256(cap * sizeof(double2));
     const size_t need = o_val + up256(cap * sizeof(double2));
     if (g.nbins >= (1ll << 31) || need > kNoAllocBytes)
         return fail(WSG_ERR_CAPACITY,
-                    "wsg_grid_noalloc: needs %zu bytes of scratch (about 24*%lld bins + 160*%ld "
+                    "wsg_grid_noalloc: needs %zu bytes of scratch (about 32*%lld bins + 161*%ld "
                     "measurements), above its fixed %zu-byte array; pass fewer measurements "
                     "per call or use the plan API",
                     need, g.nbins, num_points, kNoAllocBytes);
@@ -172,7 +174,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     BinBuffers b;
     b.ctr = reinterpret_cast<DevCounters *>(s);
     unsigned *bins = reinterpret_cast<unsigned *>(s + o_bins);
-    bin_buffer_carve(bins, g.nbins, b);
+    bin_buffer_carve(bins, g.nbins, 1, b);
     b.split_size = kDefaultSplit;
     RecBuffers r;
     r.rec16 = nullptr;
@@ -189,7 +191,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
 
     // the array keeps the previous call's contents: clear counters and bin counts
     cudaError_t e = cudaMemsetAsync(b.ctr, 0, sizeof(DevCounters), cs);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(g.nbins), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(g.nbins, b.nsub), cs);
     if (e == cudaSuccess) e = launch_bin_count(g, uu, vv, ww, num_points, b, cs);
     if (e == cudaSuccess) e = launch_bin_scan(g, b, cs);
     if (e == cudaSuccess)

@@ -56,6 +56,7 @@ struct DevCounters {
 struct GeomParams {
     int nx, ny, planes, half, tile, ntu, ntv;   // planes: all jobs' planes
     int wplanes;                                // w-planes of one job
+    int bank_pitch;                             // f32c_tile_pitch(tile, half)
     int u_pow2, w_pow2;   // dx (dw) is an exact power of two: 1/dx == 2^ku
     int ku, kw;
     double dx, dw;
@@ -67,19 +68,26 @@ struct GeomParams {
 // `split` (entry = bin | chunk << 32) and processed first.  Every other bin is
 // one work item.
 //
-// Counting uses kSub sub-counters per bin (measurement m uses sub-counter
-// (m >> 8) % kSub in both passes), which spreads the atomics of crowded bins
-// over kSub addresses.  After the scan, sub_prim[s][b] / sub_dup[s][b] hold
-// the first record position of sub-range s of bin b's primaries / duplicates
-// and the scatter advances them as cursors.
-constexpr int kSub = 8;
+// Within a bin, records are grouped into nsub sub-ranges (nsub = 1, 8 or 32,
+// a runtime property of the bin table).  A measurement's sub-range is its
+// bank class (gv * bank_pitch + gu) mod 32 (mod nsub), the same for all its
+// halo duplicates because tile edges are multiples of 32.  The sub-counters
+// spread the atomics of crowded bins over nsub addresses, and with nsub = 32
+// the FP32C tile kernels can pick, for the records of one warp pass, bank
+// classes whose shared-memory rows fall in disjoint banks.  After the scan,
+// sub_prim[s][b] / sub_dup[s][b] hold the first record position of
+// sub-range s of bin b's primaries / duplicates; the scatter advances them
+// as cursors, so afterwards they hold each sub-range's end.
+constexpr int kSubMax = 32;
+constexpr int kBankClasses = 32;
 struct BinBuffers {
-    unsigned *sub_prim, *sub_dup;            // [kSub][nbins]
+    unsigned *sub_prim, *sub_dup;            // [nsub][nbins]
     unsigned *off, *nprim, *ntotal, *is_split, *slot, *done;   // [nbins]
     unsigned long long *part;                // 2 * scan_blocks(nbins) entries
     unsigned long long *split;               // split-item list
     DevCounters *ctr;
     unsigned split_size;
+    unsigned nsub;                           // 1, 8 or 32
 };
 
 // Records.  FP32C: rec16 (16 B, see k_bin_scatter) + idx.  FP64: cell, frac,
@@ -93,23 +101,25 @@ struct RecBuffers {
     unsigned long long capacity;
 };
 
-// Bytes of BinBuffers storage for nbins bins and at most `items` split
-// items (u32 arrays, then the scan partials, then the split list; 256-byte
-// aligned).
+// Bytes of BinBuffers storage for nbins bins with nsub sub-ranges and at most
+// `items` split items (u32 arrays, then the scan partials, then the split
+// list; 256-byte aligned): (2*nsub + 6)*4 bytes per bin plus 16 per 4096 bins
+// plus 8 per split item.
 long long scan_blocks(long long nbins);
-constexpr int kBinU32PerBin = 2 * kSub + 6;
-inline size_t bin_buffer_bytes(long long nbins, unsigned long long items)
+inline size_t bin_u32_per_bin(unsigned nsub) { return 2 * (size_t)nsub + 6; }
+inline size_t bin_buffer_bytes(long long nbins, unsigned long long items, unsigned nsub)
 {
-    const size_t a = ((size_t)kBinU32PerBin * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
+    const size_t a = (bin_u32_per_bin(nsub) * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
     const size_t b = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
     return a + b + (size_t)items * 8;
 }
-inline void bin_buffer_carve(void *base, long long nbins, BinBuffers &b)
+inline void bin_buffer_carve(void *base, long long nbins, unsigned nsub, BinBuffers &b)
 {
     unsigned *u = reinterpret_cast<unsigned *>(base);
+    b.nsub = nsub;
     b.sub_prim = u;
-    b.sub_dup = u + kSub * nbins;
-    unsigned *v = u + 2 * kSub * nbins;
+    b.sub_dup = u + (size_t)nsub * nbins;
+    unsigned *v = u + 2 * (size_t)nsub * nbins;
     b.off = v;
     b.nprim = v + nbins;
     b.ntotal = v + 2 * nbins;
@@ -117,13 +127,16 @@ inline void bin_buffer_carve(void *base, long long nbins, BinBuffers &b)
     b.slot = v + 4 * nbins;
     b.done = v + 5 * nbins;
     unsigned char *c = reinterpret_cast<unsigned char *>(base);
-    const size_t a = ((size_t)kBinU32PerBin * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
+    const size_t a = (bin_u32_per_bin(nsub) * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
     const size_t p = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
     b.part = reinterpret_cast<unsigned long long *>(c + a);
     b.split = reinterpret_cast<unsigned long long *>(c + a + p);
 }
 // Bytes of the sub-counters (cleared before each binning).
-inline size_t bin_counter_bytes(long long nbins) { return (size_t)2 * kSub * nbins * sizeof(unsigned); }
+inline size_t bin_counter_bytes(long long nbins, unsigned nsub)
+{
+    return (size_t)2 * nsub * nbins * sizeof(unsigned);
+}
 // Upper bounds for `records` records cut into items of `split`: split items
 // and partial-tile slots.
 inline unsigned long long max_split_items(unsigned long long records, unsigned split)
@@ -134,6 +147,10 @@ inline unsigned long long max_slots(unsigned long long records, unsigned split)
 {
     return records / split + 1;
 }
+// Row pitch (in 4-byte words) of the FP32C gridder's shared-memory tile for
+// tile edge T and half-support K; odd, so that the rows of one support window
+// fall in distinct banks.
+__host__ __device__ constexpr int f32c_tile_pitch(int T, int K) { return (T + 4 * K) | 1; }
 
 // Pixel-geometry table of the FP32C w-correction (per pixel, planar):
 // the phase in cycles for plane w is a + w*b (mod 1), a and b as
