@@ -79,6 +79,10 @@ __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, 
     return p1 > p0;
 }
 
+// What a lane group without a record processes: cell (0, 0) of the tile, frac
+// 0, value 0 (its taps stay inside the staged tile; nothing is written).
+__device__ __constant__ const uint4 kIdleRecord = {64u << 24 | 0x800000u, 64u << 24 | 0x800000u, 0u, 0u};
+
 template <int T, int K>
 __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
 {
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
                     const unsigned cur = (cur4 >> (8 * L)) & 255u;
                     const bool valid = cur < ((cnt4 >> (8 * L)) & 255u);
                     const int slot = (warp + 8 * L) * Q + (int)cur;
-                    gather_record(stage[valid ? slot : 0], valid, valid ? sidx[slot] : 0u);
+                    gather_record(valid ? stage[slot] : kIdleRecord, valid, valid ? sidx[slot] : 0u);
                     cur4 += 0x01010101u;   // RPW = 4: every list is used once per pass
                 }
             }
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
                 for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
                     const unsigned r = base + grp;
                     const bool valid = r < cnt;
-                    gather_record(stage[valid ? r : 0], valid, valid ? sidx[r] : 0u);
+                    gather_record(valid ? stage[r] : kIdleRecord, valid, valid ? sidx[r] : 0u);
                 }
             }
         }

@@ -76,6 +76,10 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
     return b.is_split[bin] == 0u;
 }
 
+// What a lane group without a record processes: cell (0, 0) of the tile, frac
+// 0, value 0 (its addresses stay inside the accumulator; nothing is added).
+__device__ __constant__ const uint4 kIdleRecord = {64u << 24 | 0x800000u, 64u << 24 | 0x800000u, 0u, 0u};
+
 // FP32C tile kernel.  A warp pass takes RPW = 32/NT records; lane (g, k) of
 // record g owns row k of its support window: it evaluates the column weight
 // gu_k and the row weight gv_k of the separable Gaussian once, then walks the
@@ -285,8 +289,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
                     const int L = (p + grp) & 3;
                     const unsigned cur = (cur4 >> (8 * L)) & 255u;
                     const bool valid = lane_on && cur < ((cnt4 >> (8 * L)) & 255u);
-                    const uint4 q = stage[valid ? (warp + 8 * L) * Q + (int)cur : 0];
-                    scatter_record(q, valid);
+                    scatter_record(valid ? stage[(warp + 8 * L) * Q + (int)cur] : kIdleRecord, valid);
 #pragma unroll
                     for (int L2 = 0; L2 < 4; L2++)
                         if (((L2 - p) & 3) < RPW) cur4 += 1u << (8 * L2);
@@ -301,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
                 for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
                     const unsigned r = base + grp;
                     const bool valid = lane_on && r < cnt;
-                    scatter_record(stage[valid ? r : 0], valid);
+                    scatter_record(valid ? stage[r] : kIdleRecord, valid);
                 }
             }
         }
