@@ -74,20 +74,10 @@ __device__ __forceinline__ unsigned bin_index(const GeomParams &g, int w, int tv
 // operations in flight per thread.
 constexpr int kItems = 4;
 
-// The measurement's sub-range: its bank class (gv * bank_pitch + gu) mod 32,
-// reduced mod nsub (a power of two dividing 32; two's complement & is the
-// modulo for negative cells too).
-__device__ __forceinline__ unsigned sub_of(const GeomParams &g, const MGeom &o, unsigned nsub)
+__device__ __forceinline__ unsigned sub_of(long long m, unsigned nsub)
 {
-    return (unsigned)(o.gv * g.bank_pitch + o.gu) & (nsub - 1u);
+    return (unsigned)(m >> 8) & (nsub - 1u);
 }
-
-// Warp-aggregation key of a primary: (bin, sub-range); all ones = none.
-__device__ __forceinline__ unsigned long long prim_key(unsigned bin, unsigned sub)
-{
-    return ((unsigned long long)bin << 5) | sub;
-}
-constexpr unsigned long long kNoKey = ~0ull;
 
 template <bool UP2, bool WP2>
 __global__ void __launch_bounds__(256)
@@ -115,10 +105,11 @@ k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restric
             const int st = m < n ? measure<UP2, WP2, float>(g, x[i], y[i], z[i], o, fu, fv) : 3;
             ndp += st == 1;
             ndw += st == 2;
-            const unsigned sub = st == 0 ? sub_of(g, o, b.nsub) : 0u;
+            const unsigned sub = sub_of(m, b.nsub);
             const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
-            const unsigned peers = __match_any_sync(kFull, st == 0 ? prim_key(prim, sub) : kNoKey);
+            const unsigned peers = __match_any_sync(kFull, prim);
             if (st == 0) {
+                // lanes of one warp share m >> 8, hence the sub-counter
                 if (lane == __ffs(peers) - 1)
                     atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
                 for (int tv = o.tv0; tv <= o.tv1; tv++)
@@ -202,13 +193,12 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             MGeom o;
             S fu, fv;
             const int st = m < n ? measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv) : 3;
-            const unsigned sub = st == 0 ? sub_of(g, o, b.nsub) : 0u;
             const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
-            const unsigned peers = __match_any_sync(kFull, st == 0 ? prim_key(prim, sub) : kNoKey);
+            const unsigned peers = __match_any_sync(kFull, prim);
             const int leader = __ffs(peers) - 1;
             unsigned got = 0;
             if (st == 0 && lane == leader)
-                got = atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
+                got = atomicAdd(&b.sub_prim[sub_of(m, b.nsub) * nb + prim], (unsigned)__popc(peers));
             const unsigned basep = __shfl_sync(kFull, got, leader);
             ppos[i] = (st == 0) ? basep + (unsigned)__popc(peers & lt_mask) : 0xFFFFFFFFu;
         }
@@ -226,7 +216,7 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
                     const unsigned bin = bin_index(g, o.gw, tv, tu);
                     const unsigned pos = (tv == o.tvp && tu == o.tup)
                                              ? ppos[i]
-                                             : atomicAdd(&b.sub_dup[sub_of(g, o, b.nsub) * nb + bin], 1u);
+                                             : atomicAdd(&b.sub_dup[sub_of(m, b.nsub) * nb + bin], 1u);
                     const int cu = o.gu - tu * g.tile;
                     const int cv = o.gv - tv * g.tile;
                     if (PREC == WSG_FP64) {
@@ -309,11 +299,11 @@ __global__ void __launch_bounds__(256) k_bin_count_batch(GeomParams g, ChanTable
         float fu, fv;
         BatchPoint bp;
         const int st = batch_point<UP2, WP2, float>(g, t, s_m0, m, o, fu, fv, bp);
-        const unsigned sub = st == 0 ? sub_of(g, o, b.nsub) : 0u;
+        const unsigned sub = sub_of(m, b.nsub);
         for (int p = 0; p < t.pols; p++) {
             const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
             const unsigned prim = (st == 0) ? bin_index(g, plane, o.tvp, o.tup) : kFull;
-            const unsigned peers = __match_any_sync(kFull, st == 0 ? prim_key(prim, sub) : kNoKey);
+            const unsigned peers = __match_any_sync(kFull, prim);
             if (st == 0) {
                 if (lane == __ffs(peers) - 1)
                     atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
@@ -353,11 +343,11 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
         S fu, fv;
         BatchPoint bp;
         const int st = batch_point<UP2, WP2, S>(g, t, s_m0, m, o, fu, fv, bp);
-        const unsigned sub = st == 0 ? sub_of(g, o, b.nsub) : 0u;
+        const unsigned sub = sub_of(m, b.nsub);
         for (int p = 0; p < t.pols; p++) {
             const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
             const unsigned prim = (st == 0) ? bin_index(g, plane, o.tvp, o.tup) : kFull;
-            const unsigned peers = __match_any_sync(kFull, st == 0 ? prim_key(prim, sub) : kNoKey);
+            const unsigned peers = __match_any_sync(kFull, prim);
             const int leader = __ffs(peers) - 1;
             unsigned got = 0;
             if (st == 0 && lane == leader)

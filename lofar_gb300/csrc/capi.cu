@@ -109,7 +109,6 @@ int wsg::plan_configure(wsg_plan *p)
     g.ny = p->ny;
     g.half = p->half;
     g.tile = p->tile;
-    g.bank_pitch = f32c_tile_pitch(p->tile, p->half);
     g.ntu = (p->nx + p->tile - 1) / p->tile;
     g.ntv = (p->ny + p->tile - 1) / p->tile;
     g.wplanes = p->planes;
@@ -146,8 +145,7 @@ int wsg::ensure_records(wsg_plan *p, long long n)
     // a support window of <= tile cells touches at most 2x2 tiles
     const unsigned long long need = (unsigned long long)(n > 0 ? n : 1) * 4ull;
     if (need <= p->rec_cap) return WSG_OK;
-    WSG_CUDA(p->bins.ensure(bin_buffer_bytes(p->geom.nbins, max_split_items(need, p->split),
-                                             kSubMax)));
+    WSG_CUDA(p->bins.ensure(bin_buffer_bytes(p->geom.nbins, max_split_items(need, p->split), kSub)));
     if (p->prec == WSG_FP32C)
         WSG_CUDA(p->partials.ensure(max_slots(need, p->split) * (size_t)p->tile * p->tile *
                                     sizeof(float2)));

@@ -79,10 +79,6 @@ __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, 
     return p1 > p0;
 }
 
-// What a lane group without a record processes: cell (0, 0) of the tile, frac
-// 0, value 0 (its taps stay inside the staged tile; nothing is written).
-__device__ __constant__ const uint4 kIdleRecord = {64u << 24 | 0x800000u, 64u << 24 | 0x800000u, 0u, 0u};
-
 template <int T, int K>
 __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
 {
@@ -99,7 +95,6 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
     uint4 *stage = reinterpret_cast<uint4 *>(smraw + TB);
     unsigned *sidx = reinterpret_cast<unsigned *>(smraw + TB + kStage * sizeof(uint4));
     __shared__ unsigned s_item;
-    __shared__ unsigned s_cps[kBankClasses], s_cn[kBankClasses], s_nmax;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / GS, k = lane % GS;
@@ -133,99 +128,42 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
                 val = grid[(plane + (size_t)gy) * a.g.nx + (size_t)gx];
             tile[y * AP + x] = val;
         }
-        // lane group grp gathers record q: row k of its window, then the sum
-        auto gather_record = [=](const uint4 &q, bool valid, unsigned oi) {
-            const int cu = (int)(q.x >> 24) - 64;
-            const int cv = (int)(q.y >> 24) - 64;
-            const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
-            const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
-            const float du = off1 - fu, dv = off1 - fv;
-            const float gu = norm * fast_exp2(du * du * c2);
-            const float gv = on ? fast_exp2(dv * dv * c2) : 0.0f;
-            const int row = (cv - K + kk + H) * AP + (cu - K + H);
-            float sr = 0.f, si = 0.f;
-#pragma unroll
-            for (int j = 0; j < NT; j++) {
-                const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * GS + j);
-                const float2 t = tile[row + j];
-                sr = fmaf(g, t.x, sr);
-                si = fmaf(g, t.y, si);
-            }
-            sr *= gv;
-            si *= gv;
-#pragma unroll
-            for (int d = GS / 2; d >= 1; d >>= 1) {
-                sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
-                si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
-            }
-            if (k == 0 && valid) out[oi] = make_float2(sr, si);
-        };
-        if (GS == 8 && a.b.nsub == (unsigned)kBankClasses) {
-            // Bank-class order, as in the gridder: warp w takes classes w,
-            // w+8, w+16, w+24; in pass p group g takes list (p + g) mod 4, so
-            // the two records of each half-warp differ in class by 8 and
-            // their float2 rows (k*AP mod 16 distinct mod 8 for k < 8) fall
-            // in disjoint bank pairs.
-            constexpr int Q = kStage / kBankClasses;
-            if (tid < kBankClasses) {
-                const size_t nb = (size_t)a.g.nbins;
-                const unsigned c = tid, lo = off + p0, hi = off + p1;
-                const unsigned pb = c ? a.b.sub_prim[(size_t)(c - 1) * nb + bin] : off;
-                const unsigned pe = a.b.sub_prim[(size_t)c * nb + bin];
-                const unsigned ps = max(pb, lo), pe2 = min(pe, hi);
-                const unsigned np = pe2 > ps ? pe2 - ps : 0u;
-                s_cps[c] = ps;
-                s_cn[c] = np;
-                const unsigned m = __reduce_max_sync(0xFFFFFFFFu, np);
-                if (c == 0) s_nmax = m;
+        for (unsigned c0 = p0; c0 < p1; c0 += kStage) {
+            const unsigned cnt = min((unsigned)kStage, p1 - c0);
+            __syncthreads();
+            for (unsigned i = tid; i < cnt; i += kThreads) {
+                stage[i] = __ldcs(a.r.rec16 + off + c0 + i);
+                sidx[i] = __ldcs(a.r.idx + off + c0 + i);
             }
             __syncthreads();
-            const unsigned nmax = s_nmax;
-            for (unsigned base = 0; base < nmax; base += Q) {
-                __syncthreads();
-                for (int slot = tid; slot < kBankClasses * Q; slot += kThreads) {
-                    const int c = slot / Q;
-                    const unsigned v = base + (unsigned)(slot % Q);
-                    if (v < s_cn[c]) {
-                        stage[slot] = __ldcs(a.r.rec16 + s_cps[c] + v);
-                        sidx[slot] = __ldcs(a.r.idx + s_cps[c] + v);
-                    }
-                }
-                __syncthreads();
-                unsigned cnt4 = 0, cur4 = 0;
+            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
+                const unsigned r = base + grp;
+                const bool valid = r < cnt;
+                const uint4 q = stage[valid ? r : 0];
+                const int cu = (int)(q.x >> 24) - 64;
+                const int cv = (int)(q.y >> 24) - 64;
+                const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float du = off1 - fu, dv = off1 - fv;
+                const float gu = norm * fast_exp2(du * du * c2);
+                const float gv = on ? fast_exp2(dv * dv * c2) : 0.0f;
+                const int row = (cv - K + kk + H) * AP + (cu - K + H);
+                float sr = 0.f, si = 0.f;
 #pragma unroll
-                for (int L = 0; L < 4; L++) {
-                    const unsigned n = s_cn[warp + 8 * L];
-                    cnt4 |= (n > base ? min(n - base, (unsigned)Q) : 0u) << (8 * L);
+                for (int j = 0; j < NT; j++) {
+                    const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * GS + j);
+                    const float2 t = tile[row + j];
+                    sr = fmaf(g, t.x, sr);
+                    si = fmaf(g, t.y, si);
                 }
-                for (;;) {
-                    bool more = false;
+                sr *= gv;
+                si *= gv;
 #pragma unroll
-                    for (int L = 0; L < 4; L++)
-                        more |= ((cur4 >> (8 * L)) & 255u) < ((cnt4 >> (8 * L)) & 255u);
-                    if (!more) break;
-                    const int L = (int)((cur4 & 255u) + grp) & 3;   // pass number + group
-                    const unsigned cur = (cur4 >> (8 * L)) & 255u;
-                    const bool valid = cur < ((cnt4 >> (8 * L)) & 255u);
-                    const int slot = (warp + 8 * L) * Q + (int)cur;
-                    gather_record(valid ? stage[slot] : kIdleRecord, valid, valid ? sidx[slot] : 0u);
-                    cur4 += 0x01010101u;   // RPW = 4: every list is used once per pass
+                for (int d = GS / 2; d >= 1; d >>= 1) {
+                    sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
+                    si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
                 }
-            }
-        } else {
-            for (unsigned c0 = p0; c0 < p1; c0 += kStage) {
-                const unsigned cnt = min((unsigned)kStage, p1 - c0);
-                __syncthreads();
-                for (unsigned i = tid; i < cnt; i += kThreads) {
-                    stage[i] = __ldcs(a.r.rec16 + off + c0 + i);
-                    sidx[i] = __ldcs(a.r.idx + off + c0 + i);
-                }
-                __syncthreads();
-                for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
-                    const unsigned r = base + grp;
-                    const bool valid = r < cnt;
-                    gather_record(valid ? stage[r] : kIdleRecord, valid, valid ? sidx[r] : 0u);
-                }
+                if (k == 0 && valid) out[sidx[r]] = make_float2(sr, si);
             }
         }
     }

@@ -76,10 +76,6 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
     return b.is_split[bin] == 0u;
 }
 
-// What a lane group without a record processes: cell (0, 0) of the tile, frac
-// 0, value 0 (its addresses stay inside the accumulator; nothing is added).
-__device__ __constant__ const uint4 kIdleRecord = {64u << 24 | 0x800000u, 64u << 24 | 0x800000u, 0u, 0u};
-
 // FP32C tile kernel.  A warp pass takes RPW = 32/NT records; lane (g, k) of
 // record g owns row k of its support window: it evaluates the column weight
 // gu_k and the row weight gv_k of the separable Gaussian once, then walks the
@@ -120,8 +116,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
     __shared__ float s_part[NW];
     __shared__ float s_vmax[NW];
     __shared__ float s_blk[NB * NB];
-    __shared__ unsigned s_cps[kBankClasses], s_cnp[kBankClasses], s_cds[kBankClasses],
-        s_cn[kBankClasses], s_nmax;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / NT, k = lane - (lane / NT) * NT;
@@ -207,104 +201,36 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         const float scale = ldexpf(1.0f, fexp);
         const float inv = ldexpf(1.0f, -fexp);
 
-        // lane (grp, k) adds row k of record q's support window
-        auto scatter_record = [&](const uint4 &q, bool valid) {
-            const int cu = (int)(q.x >> 24) - 64;
-            const int cv = (int)(q.y >> 24) - 64;
-            const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
-            const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
-            const float du = off1 - fu, dv = off1 - fv;
-            const float gu = norm * fast_exp2(du * du * c2);
-            const float gv = fast_exp2(dv * dv * c2) * scale;
-            const float ar = __uint_as_float(q.z) * gv;
-            const float ai = __uint_as_float(q.w) * gv;
-            const int row = (cv - K + k + H) * AP + (cu - K + H);
-#pragma unroll
-            for (int j = 0; j < NT; j++) {
-                const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
-                if (valid) {
-                    // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds
-                    // it to an integer held in the low mantissa bits
-                    atomicAdd(are + row + j,
-                              __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits);
-                    atomicAdd(aim + row + j,
-                              __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits);
-                }
-            }
-        };
-        if (K >= 3 && a.b.nsub == (unsigned)kBankClasses) {
-            // Bank-class order.  Warp w takes the records of classes w, w+8,
-            // w+16, w+24 (its lists L = 0..3); in pass p, group g takes list
-            // (p + g) mod 4.  The rows of a record of class c fall in banks
-            // c + k*AP + j (mod 32) plus a constant; for k < 8 the k*AP are
-            // distinct mod 8 (AP is odd), so with NT <= 8 (support <= 7) the
-            // <= 4 records of one pass, whose classes differ by multiples of
-            // 8, hit disjoint banks (wider supports share at most one bank
-            // per row pair 8 apart).
-            constexpr int Q = kStage / kBankClasses;   // records per class per round
-            if (tid < kBankClasses) {
-                const size_t nb = (size_t)a.g.nbins;
-                const unsigned c = tid, lo = off + r0, hi = off + r1;
-                const unsigned pb = c ? a.b.sub_prim[(size_t)(c - 1) * nb + bin] : off;
-                const unsigned pe = a.b.sub_prim[(size_t)c * nb + bin];
-                const unsigned db = c ? a.b.sub_dup[(size_t)(c - 1) * nb + bin] : off + a.b.nprim[bin];
-                const unsigned de = a.b.sub_dup[(size_t)c * nb + bin];
-                const unsigned ps = max(pb, lo), pe2 = min(pe, hi);
-                const unsigned ds = max(db, lo), de2 = min(de, hi);
-                const unsigned np = pe2 > ps ? pe2 - ps : 0u;
-                const unsigned nd = de2 > ds ? de2 - ds : 0u;
-                s_cps[c] = ps;
-                s_cnp[c] = np;
-                s_cds[c] = ds;
-                s_cn[c] = np + nd;
-                const unsigned m = __reduce_max_sync(0xFFFFFFFFu, np + nd);
-                if (c == 0) s_nmax = m;
-            }
+        for (unsigned c0 = r0; c0 < r1; c0 += kStage) {
+            const unsigned cnt = min((unsigned)kStage, r1 - c0);
             __syncthreads();
-            const unsigned nmax = s_nmax;
-            for (unsigned base = 0; base < nmax; base += Q) {
-                __syncthreads();
-                for (int slot = tid; slot < kBankClasses * Q; slot += kThreads) {
-                    const int c = slot / Q;
-                    const unsigned v = base + (unsigned)(slot % Q);
-                    if (v < s_cn[c]) {
-                        const unsigned np = s_cnp[c];
-                        stage[slot] = __ldcs(rec + (v < np ? s_cps[c] + v : s_cds[c] + (v - np)));
+            for (unsigned i = tid; i < cnt; i += kThreads) stage[i] = __ldcs(rec + off + c0 + i);
+            __syncthreads();
+            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
+                const unsigned r = base + grp;
+                const bool valid = lane_on && r < cnt;
+                const uint4 q = stage[valid ? r : 0];
+                const int cu = (int)(q.x >> 24) - 64;
+                const int cv = (int)(q.y >> 24) - 64;
+                const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
+                const float du = off1 - fu, dv = off1 - fv;
+                const float gu = norm * fast_exp2(du * du * c2);
+                const float gv = fast_exp2(dv * dv * c2) * scale;
+                const float ar = __uint_as_float(q.z) * gv;
+                const float ai = __uint_as_float(q.w) * gv;
+                const int row = (cv - K + k + H) * AP + (cu - K + H);
+#pragma unroll
+                for (int j = 0; j < NT; j++) {
+                    const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
+                    if (valid) {
+                        // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds
+                        // it to an integer held in the low mantissa bits
+                        atomicAdd(are + row + j,
+                                  __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits);
+                        atomicAdd(aim + row + j,
+                                  __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits);
                     }
-                }
-                __syncthreads();
-                // packed per-list counts and cursors (one byte each, <= 40)
-                unsigned cnt4 = 0, cur4 = 0;
-#pragma unroll
-                for (int L = 0; L < 4; L++) {
-                    const unsigned n = s_cn[warp + 8 * L];
-                    cnt4 |= (n > base ? min(n - base, (unsigned)Q) : 0u) << (8 * L);
-                }
-                for (int p = 0;; p++) {
-                    bool more = false;
-#pragma unroll
-                    for (int L = 0; L < 4; L++)
-                        more |= ((cur4 >> (8 * L)) & 255u) < ((cnt4 >> (8 * L)) & 255u);
-                    if (!more) break;
-                    const int L = (p + grp) & 3;
-                    const unsigned cur = (cur4 >> (8 * L)) & 255u;
-                    const bool valid = lane_on && cur < ((cnt4 >> (8 * L)) & 255u);
-                    scatter_record(valid ? stage[(warp + 8 * L) * Q + (int)cur] : kIdleRecord, valid);
-#pragma unroll
-                    for (int L2 = 0; L2 < 4; L2++)
-                        if (((L2 - p) & 3) < RPW) cur4 += 1u << (8 * L2);
-                }
-            }
-        } else {
-            for (unsigned c0 = r0; c0 < r1; c0 += kStage) {
-                const unsigned cnt = min((unsigned)kStage, r1 - c0);
-                __syncthreads();
-                for (unsigned i = tid; i < cnt; i += kThreads) stage[i] = __ldcs(rec + off + c0 + i);
-                __syncthreads();
-                for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
-                    const unsigned r = base + grp;
-                    const bool valid = lane_on && r < cnt;
-                    scatter_record(valid ? stage[r] : kIdleRecord, valid);
                 }
             }
         }

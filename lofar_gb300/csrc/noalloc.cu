@@ -17,7 +17,7 @@
 //     nbins = num_w_planes * ceil(grid_size_y/64) * ceil(grid_size_x/64),
 // and is rejected with WSG_ERR_CAPACITY when that exceeds the array: for a
 // 4096x4096x32 grid that is about 390,000 measurements per call.  Its bin
-// table keeps one counter per bin and kind (no sub-ranges).
+// table keeps one counter per bin and kind (no sub-counters).
 //
 // All calls share the array and it keeps what the last call left in it; each
 // call clears the counters it needs before using them.  Calls whose GPU work
@@ -138,7 +138,6 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     g.wplanes = num_w_planes;
     g.half = (w_support - 1) / 2;
     g.tile = kNoAllocTile;
-    g.bank_pitch = f32c_tile_pitch(kNoAllocTile, g.half);
     g.ntu = (grid_size_x + kNoAllocTile - 1) / kNoAllocTile;
     g.ntv = (grid_size_y + kNoAllocTile - 1) / kNoAllocTile;
     g.nbins = (long long)num_w_planes * g.ntv * g.ntu;

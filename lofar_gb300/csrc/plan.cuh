@@ -112,7 +112,7 @@ struct wsg_plan {
     wsg::BinBuffers binbufs() const
     {
         wsg::BinBuffers b;
-        wsg::bin_buffer_carve(bins.p, geom.nbins, wsg::kSubMax, b);
+        wsg::bin_buffer_carve(bins.p, geom.nbins, wsg::kSub, b);
         b.ctr = ctr.as<wsg::DevCounters>();
         b.split_size = (unsigned)split;
         return b;

@@ -56,7 +56,6 @@ struct DevCounters {
 struct GeomParams {
     int nx, ny, planes, half, tile, ntu, ntv;   // planes: all jobs' planes
     int wplanes;                                // w-planes of one job
-    int bank_pitch;                             // f32c_tile_pitch(tile, half)
     int u_pow2, w_pow2;   // dx (dw) is an exact power of two: 1/dx == 2^ku
     int ku, kw;
     double dx, dw;
@@ -68,18 +67,13 @@ struct GeomParams {
 // `split` (entry = bin | chunk << 32) and processed first.  Every other bin is
 // one work item.
 //
-// Within a bin, records are grouped into nsub sub-ranges (nsub = 1, 8 or 32,
-// a runtime property of the bin table).  A measurement's sub-range is its
-// bank class (gv * bank_pitch + gu) mod 32 (mod nsub), the same for all its
-// halo duplicates because tile edges are multiples of 32.  The sub-counters
-// spread the atomics of crowded bins over nsub addresses, and with nsub = 32
-// the FP32C tile kernels can pick, for the records of one warp pass, bank
-// classes whose shared-memory rows fall in disjoint banks.  After the scan,
-// sub_prim[s][b] / sub_dup[s][b] hold the first record position of
-// sub-range s of bin b's primaries / duplicates; the scatter advances them
-// as cursors, so afterwards they hold each sub-range's end.
-constexpr int kSubMax = 32;
-constexpr int kBankClasses = 32;
+// Counting uses nsub sub-counters per bin (nsub = kSub for plans, 1 for the
+// no-allocation entry point; a power of two): measurement m uses sub-counter
+// (m >> 8) % nsub in both passes, which spreads the atomics of crowded bins
+// over nsub addresses.  After the scan, sub_prim[s][b] / sub_dup[s][b] hold
+// the first record position of sub-range s of bin b's primaries / duplicates
+// and the scatter advances them as cursors.
+constexpr int kSub = 8;
 struct BinBuffers {
     unsigned *sub_prim, *sub_dup;            // [nsub][nbins]
     unsigned *off, *nprim, *ntotal, *is_split, *slot, *done;   // [nbins]
@@ -87,7 +81,7 @@ struct BinBuffers {
     unsigned long long *split;               // split-item list
     DevCounters *ctr;
     unsigned split_size;
-    unsigned nsub;                           // 1, 8 or 32
+    unsigned nsub;
 };
 
 // Records.  FP32C: rec16 (16 B, see k_bin_scatter) + idx.  FP64: cell, frac,
@@ -101,10 +95,10 @@ struct RecBuffers {
     unsigned long long capacity;
 };
 
-// Bytes of BinBuffers storage for nbins bins with nsub sub-ranges and at most
-// `items` split items (u32 arrays, then the scan partials, then the split
-// list; 256-byte aligned): (2*nsub + 6)*4 bytes per bin plus 16 per 4096 bins
-// plus 8 per split item.
+// Bytes of BinBuffers storage for nbins bins with nsub sub-counters and at
+// most `items` split items (u32 arrays, then the scan partials, then the
+// split list; 256-byte aligned): (2*nsub + 6)*4 bytes per bin, 16 per 4096
+// bins and 8 per split item.
 long long scan_blocks(long long nbins);
 inline size_t bin_u32_per_bin(unsigned nsub) { return 2 * (size_t)nsub + 6; }
 inline size_t bin_buffer_bytes(long long nbins, unsigned long long items, unsigned nsub)
@@ -147,10 +141,6 @@ inline unsigned long long max_slots(unsigned long long records, unsigned split)
 {
     return records / split + 1;
 }
-// Row pitch (in 4-byte words) of the FP32C gridder's shared-memory tile for
-// tile edge T and half-support K; odd, so that the rows of one support window
-// fall in distinct banks.
-__host__ __device__ constexpr int f32c_tile_pitch(int T, int K) { return (T + 4 * K) | 1; }
 
 // Pixel-geometry table of the FP32C w-correction (per pixel, planar):
 // the phase in cycles for plane w is a + w*b (mod 1), a and b as
