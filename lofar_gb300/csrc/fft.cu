@@ -35,12 +35,19 @@ namespace wsg {
 
 namespace {
 
+// Complex arithmetic on the paired FP32 instructions of sm_100+ (one FADD2 /
+// FFMA2 / FMUL2 per complex add, subtract or half-product).  a - b is the
+// FFMA2 b*(-1) + a: exact product, one rounding, as a plain subtraction.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+    const float2 t = __fmul2_rn(make_float2(a.x, a.x), b);
+    return __ffma2_rn(make_float2(-a.y, a.y), make_float2(b.y, b.x), t);
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
 // a * (s i): s = +1 (exponent +i) or -1
 template <int S> __device__ __forceinline__ float2 mul_si(float2 a)
 {
@@ -295,20 +302,38 @@ __global__ void __launch_bounds__(col_group<N>() * fft_threads<N>()) k_cols(ColA
                                           : a.m.need_tile[((size_t)w * a.ntv + tv) * a.ntu + tu];
     __syncthreads();
     float2 *plane = a.grid + (size_t)w * a.ny * a.nx;
-    for (int i = tid; i < N * COLS; i += COLS * T) {
-        const int row = i / COLS, c = i % COLS;
-        float2 v = make_float2(0.f, 0.f);
-        if (MODE != kColsFwd || s_rows[row >> a.tsh])
-            v = __ldcg(plane + (size_t)row * a.nx + x0 + c);
-        cbuf[c * SC + pidx(row)] = v;
+    // each thread moves whole rows of the strip (both columns: 16 bytes); all
+    // of its loads are issued before the first shared-memory store
+    static_assert(COLS == 2, "strips of two columns");
+    constexpr int RPT = N / (COLS * T);   // rows per thread
+#pragma unroll
+    for (int h = 0; h < RPT; h += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int it = 0; it < 8; it++) {
+            const int row = tid + (h + it) * (COLS * T);
+            v[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (row < N && (MODE != kColsFwd || s_rows[row >> a.tsh]))
+                v[it] = __ldcg(reinterpret_cast<const float4 *>(plane + (size_t)row * a.nx + x0));
+        }
+#pragma unroll
+        for (int it = 0; it < 8; it++) {
+            const int row = tid + (h + it) * (COLS * T);
+            if (row < N) {
+                cbuf[pidx(row)] = make_float2(v[it].x, v[it].y);
+                cbuf[SC + pidx(row)] = make_float2(v[it].z, v[it].w);
+            }
+        }
     }
     __syncthreads();
     const int g = tid / T;
     fft_smem<N, S, T>(cbuf + g * SC, tid - g * T, a.tw);
-    for (int i = tid; i < N * COLS; i += COLS * T) {
-        const int row = i / COLS, c = i % COLS;
+#pragma unroll 4
+    for (int row = tid; row < N; row += COLS * T) {
         if (MODE == kColsAdj && !s_rows[row >> a.tsh]) continue;
-        __stcg(plane + (size_t)row * a.nx + x0 + c, cbuf[c * SC + pidx(row)]);
+        const float2 c0 = cbuf[pidx(row)], c1 = cbuf[SC + pidx(row)];
+        __stcg(reinterpret_cast<float4 *>(plane + (size_t)row * a.nx + x0),
+               make_float4(c0.x, c0.y, c1.x, c1.y));
     }
 }
 
