@@ -35,19 +35,12 @@ namespace wsg {
 
 namespace {
 
-// Complex arithmetic on the paired FP32 instructions of sm_100+ (one FADD2 /
-// FFMA2 / FMUL2 per complex add, subtract or half-product).  a - b is the
-// FFMA2 b*(-1) + a: exact product, one rounding, as a plain subtraction.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
-    const float2 t = __fmul2_rn(make_float2(a.x, a.x), b);
-    return __ffma2_rn(make_float2(-a.y, a.y), make_float2(b.y, b.x), t);
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b)
-{
-    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
-}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 // a * (s i): s = +1 (exponent +i) or -1
 template <int S> __device__ __forceinline__ float2 mul_si(float2 a)
 {
