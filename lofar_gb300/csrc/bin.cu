@@ -54,12 +54,13 @@ __device__ __forceinline__ int measure(const GeomParams &g, double x, double y, 
     o.gu = cu.g;
     o.gv = cv.g;
     o.gw = cw.g;
-    o.tu0 = ju0 / g.tile;
-    o.tu1 = ju1 / g.tile;
-    o.tv0 = jv0 / g.tile;
-    o.tv1 = jv1 / g.tile;
-    o.tup = min(max(cu.g, 0), g.nx - 1) / g.tile;
-    o.tvp = min(max(cv.g, 0), g.ny - 1) / g.tile;
+    // tile indices of non-negative cells: the tile edge is a power of two
+    o.tu0 = ju0 >> g.tile_shift;
+    o.tu1 = ju1 >> g.tile_shift;
+    o.tv0 = jv0 >> g.tile_shift;
+    o.tv1 = jv1 >> g.tile_shift;
+    o.tup = min(max(cu.g, 0), g.nx - 1) >> g.tile_shift;
+    o.tvp = min(max(cv.g, 0), g.ny - 1) >> g.tile_shift;
     return 0;
 }
 
@@ -217,8 +218,8 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
                     const unsigned pos = (tv == o.tvp && tu == o.tup)
                                              ? ppos[i]
                                              : atomicAdd(&b.sub_dup[sub_of(m, b.nsub) * nb + bin], 1u);
-                    const int cu = o.gu - tu * g.tile;
-                    const int cv = o.gv - tv * g.tile;
+                    const int cu = o.gu - (tu << g.tile_shift);
+                    const int cv = o.gv - (tv << g.tile_shift);
                     if (PREC == WSG_FP64) {
                         r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
                         reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu, fv);
@@ -369,8 +370,8 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
                     const bool primary = tv == o.tvp && tu == o.tup;
                     const unsigned pos =
                         primary ? ppos : atomicAdd(&b.sub_dup[sub * nb + bin_index(g, plane, tv, tu)], 1u);
-                    const int cu = o.gu - tu * g.tile;
-                    const int cv = o.gv - tv * g.tile;
+                    const int cu = o.gu - (tu << g.tile_shift);
+                    const int cv = o.gv - (tv << g.tile_shift);
                     if (PREC == WSG_FP64) {
                         r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
                         reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu, fv);

@@ -109,6 +109,8 @@ int wsg::plan_configure(wsg_plan *p)
     g.ny = p->ny;
     g.half = p->half;
     g.tile = p->tile;
+    g.tile_shift = 0;
+    while ((1 << g.tile_shift) < p->tile) g.tile_shift++;
     g.ntu = (p->nx + p->tile - 1) / p->tile;
     g.ntv = (p->ny + p->tile - 1) / p->tile;
     g.wplanes = p->planes;

@@ -138,6 +138,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     g.wplanes = num_w_planes;
     g.half = (w_support - 1) / 2;
     g.tile = kNoAllocTile;
+    g.tile_shift = 6;   // log2(kNoAllocTile)
     g.ntu = (grid_size_x + kNoAllocTile - 1) / kNoAllocTile;
     g.ntv = (grid_size_y + kNoAllocTile - 1) / kNoAllocTile;
     g.nbins = (long long)num_w_planes * g.ntv * g.ntu;

@@ -55,6 +55,7 @@ struct DevCounters {
 // Geometry of the coordinate step (w-stacking.cu:66-77) and the tiling.
 struct GeomParams {
     int nx, ny, planes, half, tile, ntu, ntv;   // planes: all jobs' planes
+    int tile_shift;                             // tile == 1 << tile_shift
     int wplanes;                                // w-planes of one job
     int u_pow2, w_pow2;   // dx (dw) is an exact power of two: 1/dx == 2^ku
     int ku, kw;
