@@ -177,14 +177,22 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
     const unsigned lt_mask = (1u << lane) - 1u;
     const long long stride = (long long)gridDim.x * blockDim.x * kItems;
     const long long nb = g.nbins;
+    // one frequency and one polarisation (the usual case): the value is one
+    // float product, and its inputs are loaded with the coordinates so that
+    // their latency overlaps the cursor atomics
+    const bool single = nf == 1 && np == 1;
     for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
         double x[kItems], y[kItems], z[kItems];
+        float a_re[kItems], a_im[kItems], a_wt[kItems];
 #pragma unroll
         for (int i = 0; i < kItems; i++) {
             const long long m = base + (long long)i * blockDim.x + threadIdx.x;
             x[i] = m < n ? __ldcs(uu + m) : 0.0;
             y[i] = m < n ? __ldcs(vv + m) : 0.0;
             z[i] = m < n ? __ldcs(ww + m) : 0.0;
+            a_re[i] = (single && m < n) ? __ldcs(vr + m) : 0.0f;
+            a_im[i] = (single && m < n) ? __ldcs(vi + m) : 0.0f;
+            a_wt[i] = (single && m < n) ? __ldcs(wt + m) : 0.0f;
         }
         // primary positions first (one aggregated cursor atomic per bin and warp)
         unsigned ppos[kItems];
@@ -211,7 +219,13 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             S fu, fv;
             measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv);
             S re, im;
-            fold_value<S>(vr, vi, wt, m, nf, np, re, im);
+            if (single) {
+                // the fold of w-stacking.cu:98-112 with one entry
+                re = isnan(a_re[i]) ? (S)0 : (S)(a_wt[i] * a_re[i]);
+                im = isnan(a_re[i]) ? (S)0 : (S)(a_wt[i] * a_im[i]);
+            } else {
+                fold_value<S>(vr, vi, wt, m, nf, np, re, im);
+            }
             for (int tv = o.tv0; tv <= o.tv1; tv++) {
                 for (int tu = o.tu0; tu <= o.tu1; tu++) {
                     const unsigned bin = bin_index(g, o.gw, tv, tu);
