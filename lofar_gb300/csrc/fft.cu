@@ -273,60 +273,155 @@ struct ColArgs {
     FftMasks m;
 };
 
-// Column FFTs of COLS adjacent columns of one plane (grid: x = strip, y = plane).
-template <int N, int S, int MODE>
-__global__ void __launch_bounds__(col_group<N>() * fft_threads<N>()) k_cols(ColArgs a)
+// Threads of a column-strip CTA: one per radix-16 butterfly of a column.
+template <int N> __host__ __device__ constexpr int col_threads() { return N / 16 < 512 ? N / 16 : 512; }
+
+// 16 complex values of both columns of a strip row: one 16-byte access.
+__device__ __forceinline__ float4 ld_row2(const float2 *p) { return __ldcg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ void st_row2(float2 *p, float2 a, float2 b)
 {
-    constexpr int T = fft_threads<N>();
-    constexpr int COLS = col_group<N>();
+    __stcg(reinterpret_cast<float4 *>(p), make_float4(a.x, a.y, b.x, b.y));
+}
+
+// Twiddle powers W^{r k}, r = 0..15, of one table entry W^k (a product tree
+// of depth <= 4, a few ulp).
+template <int S> __device__ __forceinline__ void twiddle_powers(float2 w1, float2 (&wp)[16])
+{
+    if (S < 0) w1.y = -w1.y;
+    wp[0] = make_float2(1.f, 0.f);
+    wp[1] = w1;
+    wp[2] = cmul(w1, w1);
+    wp[3] = cmul(wp[2], w1);
+    wp[4] = cmul(wp[2], wp[2]);
+#pragma unroll
+    for (int r = 5; r < 8; r++) wp[r] = cmul(wp[4], wp[r - 4]);
+    wp[8] = cmul(wp[4], wp[4]);
+#pragma unroll
+    for (int r = 9; r < 12; r++) wp[r] = cmul(wp[8], wp[r - 8]);
+    wp[12] = cmul(wp[8], wp[4]);
+#pragma unroll
+    for (int r = 13; r < 16; r++) wp[r] = cmul(wp[12], wp[r - 12]);
+}
+
+// Column FFTs of a strip of two adjacent columns of one plane (grid: x =
+// strip, y = plane).  Thread t owns butterfly t of every radix-16 pass of both
+// columns (same twiddles).  The first pass reads its 16 inputs straight from
+// HBM (rows t + r*N/16) and the last pass writes its 16 (or R) outputs straight
+// back, so shared memory only carries the passes in between: 4 shared-memory
+// accesses per point instead of 8 with staged loads and stores.  Forward:
+// rows of tiles without measurements are zero and not read.  Adjoint: only
+// rows of tiles the degridder reads are written.
+template <int N, int S, int MODE>
+__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 : 1) k_cols(ColArgs a)
+{
+    constexpr int T = col_threads<N>();
+    constexpr int L16 = FftPlan<N>::L16;
+    constexpr int R = FftPlan<N>::R;
+    constexpr int NB = N / 16;
+    static_assert(NB == T, "one radix-16 butterfly per thread");
+    static_assert(L16 >= 2, "at least two radix-16 passes");
     constexpr int SC = col_stride<N>();
     extern __shared__ __align__(16) float2 cbuf[];
+    float2 *ca = cbuf, *cb = cbuf + SC;
     const int w = blockIdx.y;
-    const int x0 = blockIdx.x * COLS;
+    const int x0 = blockIdx.x * 2;
     const int tu = x0 >> a.tsh;
     if (MODE == kColsFwd && !a.m.occ_col[w * a.ntu + tu]) return;   // strip stays zero
     if (MODE == kColsAdj && !a.m.need_col[w * a.ntu + tu]) return;  // never read
     // this strip's tile-row mask (forward: tiles read; adjoint: tiles written)
     __shared__ unsigned char s_rows[N / 16];
-    const int tid = threadIdx.x;
+    const int t = threadIdx.x;
     if (MODE != kColsPlain)
-        for (int tv = tid; tv < a.ntv; tv += COLS * T)
+        for (int tv = t; tv < a.ntv; tv += T)
             s_rows[tv] = MODE == kColsFwd ? a.m.occ_tile[((size_t)w * a.ntv + tv) * a.ntu + tu]
                                           : a.m.need_tile[((size_t)w * a.ntv + tv) * a.ntu + tu];
     __syncthreads();
-    float2 *plane = a.grid + (size_t)w * a.ny * a.nx;
-    // each thread moves whole rows of the strip (both columns: 16 bytes); all
-    // of its loads are issued before the first shared-memory store
-    static_assert(COLS == 2, "strips of two columns");
-    constexpr int RPT = N / (COLS * T);   // rows per thread
+    float2 *col = a.grid + (size_t)w * a.ny * a.nx + x0;
+    const size_t pitch = (size_t)a.nx;
+
+    // pass 0 (no twiddles): rows t + r*NB from HBM, outputs to 16t + r
+    {
+        float2 xa[16], xb[16];
 #pragma unroll
-    for (int h = 0; h < RPT; h += 8) {
-        float4 v[8];
-#pragma unroll
-        for (int it = 0; it < 8; it++) {
-            const int row = tid + (h + it) * (COLS * T);
-            v[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (row < N && (MODE != kColsFwd || s_rows[row >> a.tsh]))
-                v[it] = __ldcg(reinterpret_cast<const float4 *>(plane + (size_t)row * a.nx + x0));
+        for (int r = 0; r < 16; r++) {
+            const int row = t + r * NB;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (MODE != kColsFwd || s_rows[row >> a.tsh]) v = ld_row2(col + (size_t)row * pitch);
+            xa[r] = make_float2(v.x, v.y);
+            xb[r] = make_float2(v.z, v.w);
         }
+        dft16<S>(xa);
+        dft16<S>(xb);
 #pragma unroll
-        for (int it = 0; it < 8; it++) {
-            const int row = tid + (h + it) * (COLS * T);
-            if (row < N) {
-                cbuf[pidx(row)] = make_float2(v[it].x, v[it].y);
-                cbuf[SC + pidx(row)] = make_float2(v[it].z, v[it].w);
-            }
+        for (int r = 0; r < 16; r++) {
+            ca[pidx(16 * t + r)] = xa[r];
+            cb[pidx(16 * t + r)] = xb[r];
         }
     }
     __syncthreads();
-    const int g = tid / T;
-    fft_smem<N, S, T>(cbuf + g * SC, tid - g * T, a.tw);
-#pragma unroll 4
-    for (int row = tid; row < N; row += COLS * T) {
-        if (MODE == kColsAdj && !s_rows[row >> a.tsh]) continue;
-        const float2 c0 = cbuf[pidx(row)], c1 = cbuf[SC + pidx(row)];
-        __stcg(reinterpret_cast<float4 *>(plane + (size_t)row * a.nx + x0),
-               make_float4(c0.x, c0.y, c1.x, c1.y));
+    int ns = 16;
+#pragma unroll
+    for (int p = 1; p < L16; p++) {
+        const bool last = (p == L16 - 1) && R == 1;
+        const int k = t % ns;
+        float2 xa[16], xb[16], wp[16];
+        twiddle_powers<S>(__ldg(a.tw + k * (N / (16 * ns))), wp);
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+            xa[r] = cmul(ca[pidx(t + r * NB)], wp[r]);
+            xb[r] = cmul(cb[pidx(t + r * NB)], wp[r]);
+        }
+        dft16<S>(xa);
+        dft16<S>(xb);
+        if (last) {
+            // t / ns == 0: outputs go to rows t + r*ns = t + r*NB
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                const int row = t + r * NB;
+                if (MODE != kColsAdj || s_rows[row >> a.tsh])
+                    st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+            }
+        } else {
+            __syncthreads();
+            const int base = (t / ns) * ns * 16 + k;
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                ca[pidx(base + r * ns)] = xa[r];
+                cb[pidx(base + r * ns)] = xb[r];
+            }
+            __syncthreads();
+        }
+        ns *= 16;
+    }
+    if constexpr (R > 1) {
+        // last pass, radix R: ns = N/R, butterflies j < N/R, outputs to rows j + r*N/R
+        constexpr int NBR = N / R;
+        constexpr int BPT = NBR / T;
+#pragma unroll
+        for (int b = 0; b < BPT; b++) {
+            const int j = t + b * T;
+            float2 xa[16], xb[16];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                float2 va = ca[pidx(j + r * NBR)], vb = cb[pidx(j + r * NBR)];
+                if (r > 0) {
+                    float2 wv = __ldg(a.tw + r * j);   // W_N^{r j}: k = j, step 1
+                    if (S < 0) wv.y = -wv.y;
+                    va = cmul(va, wv);
+                    vb = cmul(vb, wv);
+                }
+                xa[r] = va;
+                xb[r] = vb;
+            }
+            dft_small<S, R>(xa);
+            dft_small<S, R>(xb);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int row = j + r * NBR;
+                if (MODE != kColsAdj || s_rows[row >> a.tsh])
+                    st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+            }
+        }
     }
 }
 
@@ -569,7 +664,7 @@ __global__ void k_twiddles(float2 *tw, int n)
     }
 }
 
-template <int N> size_t col_smem() { return (size_t)col_group<N>() * col_stride<N>() * sizeof(float2); }
+template <int N> size_t col_smem() { return (size_t)2 * col_stride<N>() * sizeof(float2); }
 template <int N> size_t row_smem(int planes, int ntu)
 {
     return ((FftPlan<N>::PAD * 8 + 15) / 16) * 16 + (size_t)4 * N * sizeof(float) +
@@ -583,7 +678,7 @@ cudaError_t run_cols(const ColArgs &a, int planes, cudaStream_t s)
     cudaError_t e = cudaFuncSetAttribute(k_cols<N, S, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_cols<N, S, MODE><<<dim3(a.nx / col_group<N>(), planes), col_group<N>() * fft_threads<N>(),
+    k_cols<N, S, MODE><<<dim3(a.nx / 2, planes), col_threads<N>(),
                          smem, s>>>(a);
     return cudaGetLastError();
 }
