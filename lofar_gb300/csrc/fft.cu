@@ -249,6 +249,123 @@ __device__ __forceinline__ void fft_smem(float2 *buf, int t, const float2 *__res
 }
 
 
+// Twiddle powers W^{r k}, r = 0..15, of one table entry W^k (a product tree
+// of depth <= 4, a few ulp).
+template <int S> __device__ __forceinline__ void twiddle_powers(float2 w1, float2 (&wp)[16])
+{
+    if (S < 0) w1.y = -w1.y;
+    wp[0] = make_float2(1.f, 0.f);
+    wp[1] = w1;
+    wp[2] = cmul(w1, w1);
+    wp[3] = cmul(wp[2], w1);
+    wp[4] = cmul(wp[2], wp[2]);
+#pragma unroll
+    for (int r = 5; r < 8; r++) wp[r] = cmul(wp[4], wp[r - 4]);
+    wp[8] = cmul(wp[4], wp[4]);
+#pragma unroll
+    for (int r = 9; r < 12; r++) wp[r] = cmul(wp[8], wp[r - 8]);
+    wp[12] = cmul(wp[8], wp[4]);
+#pragma unroll
+    for (int r = 13; r < 16; r++) wp[r] = cmul(wp[12], wp[r - 12]);
+}
+
+// The same transform for a CTA of T threads whose thread t holds the values
+// of indices t + q*T (q < N/T) in registers: with IN_REGS the first radix-16
+// pass takes its inputs from v (butterfly j = t + b*T reads indices
+// j + r*N/16, i.e. q = b + r*(N/16)/T), and with OUT_REGS the last pass leaves
+// its outputs in v in the same layout; shared memory then carries only the
+// passes in between.  Without IN_REGS the input is in buf (caller
+// synchronises before); without OUT_REGS the output is in buf.  The caller
+// synchronises before a call whose first pass writes buf while other threads
+// may still read it.
+template <int N, int S, int T, bool IN_REGS, bool OUT_REGS>
+__device__ __forceinline__ void fft_row(float2 (&v)[N / T], float2 *buf, int t,
+                                        const float2 *__restrict__ tw)
+{
+    constexpr int L16 = FftPlan<N>::L16;
+    constexpr int R = FftPlan<N>::R;
+    constexpr int NB = N / 16;
+    constexpr int BPT = NB / T;
+    static_assert(BPT * T == NB, "T divides the butterfly count");
+    int ns = 1;
+#pragma unroll
+    for (int p = 0; p < L16; p++) {
+        const bool from_regs = IN_REGS && p == 0;
+        const bool to_regs = OUT_REGS && R == 1 && p == L16 - 1;
+        float2 x[16][BPT];
+#pragma unroll
+        for (int b = 0; b < BPT; b++) {
+            const int j = t + b * T;
+            const int k = j % ns;
+#pragma unroll
+            for (int r = 0; r < 16; r++) x[r][b] = from_regs ? v[b + r * BPT] : buf[pidx(j + r * NB)];
+            if (ns > 1) {
+                float2 wp[16];
+                twiddle_powers<S>(__ldg(tw + k * (N / (16 * ns))), wp);
+#pragma unroll
+                for (int r = 1; r < 16; r++) x[r][b] = cmul(x[r][b], wp[r]);
+            }
+        }
+        if (!from_regs && !to_regs) __syncthreads();
+#pragma unroll
+        for (int b = 0; b < BPT; b++) {
+            const int j = t + b * T;
+            const int k = j % ns;
+            float2 y[16];
+#pragma unroll
+            for (int r = 0; r < 16; r++) y[r] = x[r][b];
+            dft16<S>(y);
+            if (to_regs) {
+                // ns = N/16: outputs j + r*N/16
+#pragma unroll
+                for (int r = 0; r < 16; r++) v[b + r * BPT] = y[r];
+            } else {
+                const int base = (j / ns) * ns * 16 + k;
+#pragma unroll
+                for (int r = 0; r < 16; r++) buf[pidx(base + r * ns)] = y[r];
+            }
+        }
+        if (!to_regs) __syncthreads();
+        ns *= 16;
+    }
+    if constexpr (R > 1) {
+        // ns = N/R: butterflies j < N/R, outputs j + r*N/R
+        constexpr int NBR = N / R;
+        constexpr int BPR = NBR / T;
+        static_assert(BPR * T == NBR, "T divides the last pass");
+        float2 x[R][BPR];
+#pragma unroll
+        for (int b = 0; b < BPR; b++) {
+            const int j = t + b * T;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                float2 u = buf[pidx(j + r * NBR)];
+                if (r > 0) {
+                    float2 wv = __ldg(tw + r * j);
+                    if (S < 0) wv.y = -wv.y;
+                    u = cmul(u, wv);
+                }
+                x[r][b] = u;
+            }
+        }
+        if (!OUT_REGS) __syncthreads();
+#pragma unroll
+        for (int b = 0; b < BPR; b++) {
+            const int j = t + b * T;
+            float2 y[16];
+#pragma unroll
+            for (int r = 0; r < R; r++) y[r] = x[r][b];
+            dft_small<S, R>(y);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                if (OUT_REGS) v[b + r * BPR] = y[r];
+                else buf[pidx(j + r * NBR)] = y[r];
+            }
+        }
+        if (!OUT_REGS) __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
@@ -281,26 +398,6 @@ __device__ __forceinline__ float4 ld_row2(const float2 *p) { return __ldcg(reint
 __device__ __forceinline__ void st_row2(float2 *p, float2 a, float2 b)
 {
     __stcg(reinterpret_cast<float4 *>(p), make_float4(a.x, a.y, b.x, b.y));
-}
-
-// Twiddle powers W^{r k}, r = 0..15, of one table entry W^k (a product tree
-// of depth <= 4, a few ulp).
-template <int S> __device__ __forceinline__ void twiddle_powers(float2 w1, float2 (&wp)[16])
-{
-    if (S < 0) w1.y = -w1.y;
-    wp[0] = make_float2(1.f, 0.f);
-    wp[1] = w1;
-    wp[2] = cmul(w1, w1);
-    wp[3] = cmul(wp[2], w1);
-    wp[4] = cmul(wp[2], wp[2]);
-#pragma unroll
-    for (int r = 5; r < 8; r++) wp[r] = cmul(wp[4], wp[r - 4]);
-    wp[8] = cmul(wp[4], wp[4]);
-#pragma unroll
-    for (int r = 9; r < 12; r++) wp[r] = cmul(wp[8], wp[r - 8]);
-    wp[12] = cmul(wp[8], wp[4]);
-#pragma unroll
-    for (int r = 13; r < 16; r++) wp[r] = cmul(wp[12], wp[r - 12]);
 }
 
 // Column FFTs of a strip of two adjacent columns of one plane (grid: x =
@@ -502,12 +599,13 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
         while (wn < a.planes && !plane_occ[wn]) wn++;
         if (wn < a.planes) fetch(wn);
         __syncthreads();
-        fft_smem<N, +1, T>(buf, t, a.tw);
+        float2 fv[Q];
+        fft_row<N, +1, T, false, true>(fv, buf, t, a.tw);   // transformed row in registers
         const float wf = (float)w;
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const int x = t + q * T;
-            const float2 v = buf[pidx(x)];
+            const float2 v = fv[q];
             if (a.phase) {
                 const float c = cycle_frac_f(wah[x], wal[x], wbh[x], wbl[x], wf);
                 float sn, cs;
@@ -572,10 +670,11 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
             im[q] = make_float2(v.x * amp, v.y * amp);
         }
     }
+    __syncthreads();   // shared w-screen and masks loaded
     for (int w = 0; w < a.planes; w++) {
         if (!plane_need[w]) continue;
-        __syncthreads();
         const float wf = (float)w;
+        float2 fv[Q];   // the phased row, then (in place) its transform
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const int x = t + q * T;
@@ -586,13 +685,16 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
                 __sincosf(kTwoPi * c, &sn, &cs);
                 v = make_float2(cs * im[q].x + sn * im[q].y, cs * im[q].y - sn * im[q].x);
             }
-            buf[pidx(x)] = v;
+            fv[q] = v;
         }
-        __syncthreads();
-        fft_smem<N, -1, T>(buf, t, a.tw);
+        __syncthreads();   // the previous plane's last pass has read buf
+        fft_row<N, -1, T, true, true>(fv, buf, t, a.tw);
         float2 *dst = gridj + ((size_t)w * a.ny + y) * N;
-        for (int x = t; x < N; x += T)
-            if (smask[w * a.ntu + (x >> a.tsh)]) __stcg(dst + x, buf[pidx(x)]);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int x = t + q * T;
+            if (smask[w * a.ntu + (x >> a.tsh)]) __stcg(dst + x, fv[q]);
+        }
     }
 }
 
