@@ -592,15 +592,14 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
     };
     if (w < a.planes) fetch(w);
     while (w < a.planes) {
-        __syncthreads();
+        float2 fv[Q];
 #pragma unroll
-        for (int q = 0; q < Q; q++) buf[pidx(t + q * T)] = nxt[q];
+        for (int q = 0; q < Q; q++) fv[q] = nxt[q];
         int wn = w + 1;
         while (wn < a.planes && !plane_occ[wn]) wn++;
         if (wn < a.planes) fetch(wn);
-        __syncthreads();
-        float2 fv[Q];
-        fft_row<N, +1, T, false, true>(fv, buf, t, a.tw);   // transformed row in registers
+        __syncthreads();   // the previous plane's last pass has read buf
+        fft_row<N, +1, T, true, true>(fv, buf, t, a.tw);   // the row in and out of registers
         const float wf = (float)w;
 #pragma unroll
         for (int q = 0; q < Q; q++) {
