@@ -46,13 +46,6 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
     lo += e;
 }
 
-// Predicated atomic add to a 32-bit shared-memory address (no branch).
-__device__ __forceinline__ void red_shared_if(unsigned addr, int v, bool p)
-{
-    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q red.shared.add.s32 [%0], %1;\n\t}"
-                 :: "r"(addr), "r"(v), "r"((int)p) : "memory");
-}
-
 constexpr float kRoundMagic = 12582912.0f;   // 1.5 * 2^23
 constexpr int kRoundMagicBits = 0x4B400000;    // its bit pattern
 
@@ -83,19 +76,13 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
     return b.is_split[bin] == 0u;
 }
 
-// FP32C tile kernel.  A warp takes one record at a time (warp w of the CTA
-// takes the staged records w, w + NW, ...; records are staged kStage at a time
-// with coalesced 16-byte loads).  Lane l = CG*k + c (CG = 32/NT column groups)
-// owns row k of the record's support window and its columns c, c + CG, ...:
-// one pass per column group.  Lanes 0..NT-1 evaluate the NT column weights and
-// lanes 16..16+NT-1 the NT row weights of the separable Gaussian (one
-// exponential each); the others take them by shuffle.
-//
-// The accumulator holds the tile's T x T interior only, at row pitch
-// AP = T + CG: the taps of one pass fall at banks k*CG + c + const (mod 32),
-// all distinct, so a warp's shared-memory atomics never conflict.  Taps
-// outside the tile (from the halo duplicates of neighbouring tiles' records,
-// or beyond the grid edge) are skipped by predicate.
+// FP32C tile kernel.  A warp pass takes RPW = 32/NT records; lane (g, k) of
+// record g owns row k of its support window: it evaluates the column weight
+// gu_k and the row weight gv_k of the separable Gaussian once, then walks the
+// NT columns of its row, fetching gu_j from lane (g, j) with a shuffle and
+// adding V*gv_k*gu_j into the shared-memory accumulator (odd pitch: the NT
+// rows of one record fall in distinct banks).  Records are staged into shared
+// memory kStage at a time with coalesced 16-byte loads.
 //
 // The accumulator is int32 fixed point: shared-memory integer atomics retire
 // about five times faster than float ones on this part.  Each work item first
@@ -104,47 +91,46 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
 // the rounding of each term.  The integer sums are exact and
 // order-independent; the only error is the rounding of each tap to the
 // item's quantum, 2^-f.
+//
+// The accumulator has a 2K halo on every side so that every tap of every
+// record of the bin lands in it without a bounds test; the halo is never read
+// and is not cleared (it only collects the taps of neighbouring tiles).
 template <int T, int K>
 __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
 {
     constexpr int NT = 2 * K + 1;
-    constexpr int CG = 32 / NT;              // column groups: NT*CG <= 32 lanes
-    constexpr int NP = (NT + CG - 1) / CG;   // passes over the columns
-    constexpr int AP = T + CG;               // accumulator row pitch (words)
+    constexpr int RPW = 32 / NT;
     constexpr int H = 2 * K;
-    constexpr int AW = T + 2 * H;            // bound blocks cover centres in [-H, T+H)
+    constexpr int AW = T + 2 * H;
+    constexpr int AP = AW | 1;
     constexpr int NW = kThreads / 32;
     constexpr int CPT = T * T / kThreads;
-    constexpr int ACC = ((2 * T * AP * 4) + 15) / 16 * 16;
-    static_assert(NT <= 16, "row and column weights fit in one warp");
+    constexpr int ACC = ((2 * AW * AP * 4) + 15) / 16 * 16;
     extern __shared__ __align__(16) unsigned char smraw[];
     int *are = reinterpret_cast<int *>(smraw);
-    int *aim = are + T * AP;
+    int *aim = are + AW * AP;
     uint4 *stage = reinterpret_cast<uint4 *>(smraw + ACC);
     __shared__ unsigned s_item;
     __shared__ int s_last;
-    constexpr int NB = (AW + 7) / 8;   // 8x8-cell blocks of the record centres
+    constexpr int NB = (AW + 7) / 8;   // 8x8-cell blocks of the accumulator
     __shared__ float s_part[NW];
     __shared__ float s_vmax[NW];
     __shared__ float s_blk[NB * NB];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int kr = lane / CG, cg = lane - (lane / CG) * CG;   // row, column group
-    const bool row_on = kr < NT;
-    const int wl = lane & 15;                 // weight lane: column (< 16) or row (>= 16) wl
-    const bool is_row_w = lane >= 16;
-    const float offw = (float)(wl - K) + 0.5f;
+    const int grp = lane / NT, k = lane - (lane / NT) * NT;
+    const bool lane_on = grp < RPW;
     const float norm = (float)(0.5 / kRefPi);
     const float c2 = -0.72134752044448170368f;   // -0.5 * log2(e)
+    const float off1 = (float)(k - K) + 0.5f;
     const uint4 *__restrict__ rec = a.r.rec16;
     float2 *grid = reinterpret_cast<float2 *>(a.grid);
     float2 *parts = reinterpret_cast<float2 *>(a.partials);
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
     const unsigned split = a.b.split_size;
-    const unsigned sre = (unsigned)__cvta_generic_to_shared(are);
 
-    for (int i = tid; i < 2 * T * AP; i += kThreads) are[i] = 0;
+    for (int i = tid; i < 2 * AW * AP; i += kThreads) are[i] = 0;
 
     for (;;) {
         __syncthreads();
@@ -220,33 +206,31 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
             __syncthreads();
             for (unsigned i = tid; i < cnt; i += kThreads) stage[i] = __ldcs(rec + off + c0 + i);
             __syncthreads();
-            for (unsigned r = warp; r < cnt; r += NW) {
-                const uint4 q = stage[r];
+            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
+                const unsigned r = base + grp;
+                const bool valid = lane_on && r < cnt;
+                const uint4 q = stage[valid ? r : 0];
                 const int cu = (int)(q.x >> 24) - 64;
                 const int cv = (int)(q.y >> 24) - 64;
                 const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
-                // lane wl: column weight gu_wl (lanes < 16) or row weight gv_wl (>= 16)
-                const float d = offw - (is_row_w ? fv : fu);
-                const float gw = fast_exp2(d * d * c2) * (is_row_w ? scale : norm);
-                const float gv = __shfl_sync(0xFFFFFFFFu, gw, 16 + (row_on ? kr : 0));
+                const float du = off1 - fu, dv = off1 - fv;
+                const float gu = norm * fast_exp2(du * du * c2);
+                const float gv = fast_exp2(dv * dv * c2) * scale;
                 const float ar = __uint_as_float(q.z) * gv;
                 const float ai = __uint_as_float(q.w) * gv;
-                const int row = cv - K + kr;        // tile-relative cell of this lane
-                const int col = cu - K + cg;
-                const bool rok = row_on && (unsigned)row < (unsigned)T;
-                const unsigned adr = sre + 4u * (unsigned)(row * AP + col);
+                const int row = (cv - K + k + H) * AP + (cu - K + H);
 #pragma unroll
-                for (int p = 0; p < NP; p++) {
-                    const int j = cg + p * CG;
-                    const float g = __shfl_sync(0xFFFFFFFFu, gw, j < NT ? j : 0);
-                    const bool ok = rok && j < NT && (unsigned)(col + p * CG) < (unsigned)T;
-                    // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds it
-                    // to an integer held in the low mantissa bits
-                    const int tr = __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits;
-                    const int ti = __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits;
-                    red_shared_if(adr + 4u * (unsigned)(p * CG), tr, ok);
-                    red_shared_if(adr + 4u * (unsigned)(p * CG + T * AP), ti, ok);
+                for (int j = 0; j < NT; j++) {
+                    const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
+                    if (valid) {
+                        // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds
+                        // it to an integer held in the low mantissa bits
+                        atomicAdd(are + row + j,
+                                  __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits);
+                        atomicAdd(aim + row + j,
+                                  __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits);
+                    }
                 }
             }
         }
@@ -260,7 +244,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         for (int i = 0; i < CPT; i++) {
             const int c = tid + i * kThreads;
             const int y = c / T, x = c % T;
-            const int idx = y * AP + x;
+            const int idx = (y + H) * AP + x + H;
             const float2 v = make_float2((float)are[idx] * inv, (float)aim[idx] * inv);
             are[idx] = 0;
             aim[idx] = 0;
@@ -393,8 +377,9 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
 template <int T, int K> size_t grid_smem(int prec)
 {
     if (prec == WSG_FP64) return (size_t)2 * T * (T + 2 * K + 1) * sizeof(double);
-    constexpr int AP = T + 32 / (2 * K + 1);
-    return ((size_t)(2 * T * AP * 4) + 15) / 16 * 16 + (size_t)kStage * sizeof(uint4);
+    constexpr int AW = T + 4 * K;
+    constexpr int AP = AW | 1;
+    return ((size_t)(2 * AW * AP * 4) + 15) / 16 * 16 + (size_t)kStage * sizeof(uint4);
 }
 
 template <int T, int K> const void *grid_kernel(int prec)
