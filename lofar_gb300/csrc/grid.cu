@@ -46,13 +46,6 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
     lo += e;
 }
 
-// Atomic add to a 32-bit shared-memory address under a predicate (no branch).
-__device__ __forceinline__ void red_shared_if(unsigned addr, int v, bool p)
-{
-    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q red.shared.add.s32 [%0], %1;\n\t}"
-                 :: "r"(addr), "r"(v), "r"((int)p) : "memory");
-}
-
 constexpr float kRoundMagic = 12582912.0f;   // 1.5 * 2^23
 constexpr int kRoundMagicBits = 0x4B400000;    // its bit pattern
 
@@ -137,7 +130,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
     const unsigned split = a.b.split_size;
 
-    const unsigned sre = (unsigned)__cvta_generic_to_shared(are);
     for (int i = tid; i < 2 * AW * AP; i += kThreads) are[i] = 0;
 
     for (;;) {
@@ -228,16 +220,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
                 const float ar = __uint_as_float(q.z) * gv;
                 const float ai = __uint_as_float(q.w) * gv;
                 const int row = (cv - K + k + H) * AP + (cu - K + H);
-                const unsigned adr = sre + 4u * (unsigned)row;
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
                     const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
-                    // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds it
-                    // to an integer held in the low mantissa bits
-                    const int tr = __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits;
-                    const int ti = __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits;
-                    red_shared_if(adr + 4u * (unsigned)j, tr, valid);
-                    red_shared_if(adr + 4u * (unsigned)(j + AW * AP), ti, valid);
+                    if (valid) {
+                        // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds
+                        // it to an integer held in the low mantissa bits
+                        atomicAdd(are + row + j,
+                                  __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits);
+                        atomicAdd(aim + row + j,
+                                  __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits);
+                    }
                 }
             }
         }
