@@ -400,7 +400,10 @@ __device__ __forceinline__ void st_row2(float2 *p, float2 a, float2 b)
     __stcg(reinterpret_cast<float4 *>(p), make_float4(a.x, a.y, b.x, b.y));
 }
 
-// Column FFTs of a strip of two adjacent columns of one plane (grid: x =
+// Columns per column-FFT CTA (1 or 2).
+constexpr int kColsPerCta = 2;
+
+// Column FFTs of a strip of kColsPerCta adjacent columns of one plane (grid: x =
 // strip, y = plane).  Thread t owns butterfly t of every radix-16 pass of both
 // columns (same twiddles).  The first pass reads its 16 inputs straight from
 // HBM (rows t + r*N/16) and the last pass writes its 16 (or R) outputs straight
@@ -409,8 +412,9 @@ __device__ __forceinline__ void st_row2(float2 *p, float2 a, float2 b)
 // rows of tiles without measurements are zero and not read.  Adjoint: only
 // rows of tiles the degridder reads are written.
 template <int N, int S, int MODE>
-__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 : 1) k_cols(ColArgs a)
+__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (kColsPerCta == 2 ? 2 : 3) : 1) k_cols(ColArgs a)
 {
+    constexpr int NC = kColsPerCta;
     constexpr int T = col_threads<N>();
     constexpr int L16 = FftPlan<N>::L16;
     constexpr int R = FftPlan<N>::R;
@@ -421,7 +425,7 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 
     extern __shared__ __align__(16) float2 cbuf[];
     float2 *ca = cbuf, *cb = cbuf + SC;
     const int w = blockIdx.y;
-    const int x0 = blockIdx.x * 2;
+    const int x0 = blockIdx.x * NC;
     const int tu = x0 >> a.tsh;
     if (MODE == kColsFwd && !a.m.occ_col[w * a.ntu + tu]) return;   // strip stays zero
     if (MODE == kColsAdj && !a.m.need_col[w * a.ntu + tu]) return;  // never read
@@ -442,17 +446,22 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             const int row = t + r * NB;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (MODE != kColsFwd || s_rows[row >> a.tsh]) v = ld_row2(col + (size_t)row * pitch);
-            xa[r] = make_float2(v.x, v.y);
-            xb[r] = make_float2(v.z, v.w);
+            if (NC == 2) {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (MODE != kColsFwd || s_rows[row >> a.tsh]) v = ld_row2(col + (size_t)row * pitch);
+                xa[r] = make_float2(v.x, v.y);
+                xb[r] = make_float2(v.z, v.w);
+            } else {
+                xa[r] = make_float2(0.f, 0.f);
+                if (MODE != kColsFwd || s_rows[row >> a.tsh]) xa[r] = __ldcg(col + (size_t)row * pitch);
+            }
         }
         dft16<S>(xa);
-        dft16<S>(xb);
+        if (NC == 2) dft16<S>(xb);
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             ca[pidx(16 * t + r)] = xa[r];
-            cb[pidx(16 * t + r)] = xb[r];
+            if (NC == 2) cb[pidx(16 * t + r)] = xb[r];
         }
     }
     __syncthreads();
@@ -466,17 +475,19 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             xa[r] = cmul(ca[pidx(t + r * NB)], wp[r]);
-            xb[r] = cmul(cb[pidx(t + r * NB)], wp[r]);
+            if (NC == 2) xb[r] = cmul(cb[pidx(t + r * NB)], wp[r]);
         }
         dft16<S>(xa);
-        dft16<S>(xb);
+        if (NC == 2) dft16<S>(xb);
         if (last) {
             // t / ns == 0: outputs go to rows t + r*ns = t + r*NB
 #pragma unroll
             for (int r = 0; r < 16; r++) {
                 const int row = t + r * NB;
-                if (MODE != kColsAdj || s_rows[row >> a.tsh])
-                    st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+                if (MODE != kColsAdj || s_rows[row >> a.tsh]) {
+                    if (NC == 2) st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+                    else __stcg(col + (size_t)row * pitch, xa[r]);
+                }
             }
         } else {
             __syncthreads();
@@ -484,7 +495,7 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 
 #pragma unroll
             for (int r = 0; r < 16; r++) {
                 ca[pidx(base + r * ns)] = xa[r];
-                cb[pidx(base + r * ns)] = xb[r];
+                if (NC == 2) cb[pidx(base + r * ns)] = xb[r];
             }
             __syncthreads();
         }
@@ -500,23 +511,26 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? 2 
             float2 xa[16], xb[16];
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                float2 va = ca[pidx(j + r * NBR)], vb = cb[pidx(j + r * NBR)];
+                float2 va = ca[pidx(j + r * NBR)];
+                float2 vb = NC == 2 ? cb[pidx(j + r * NBR)] : make_float2(0.f, 0.f);
                 if (r > 0) {
                     float2 wv = __ldg(a.tw + r * j);   // W_N^{r j}: k = j, step 1
                     if (S < 0) wv.y = -wv.y;
                     va = cmul(va, wv);
-                    vb = cmul(vb, wv);
+                    if (NC == 2) vb = cmul(vb, wv);
                 }
                 xa[r] = va;
                 xb[r] = vb;
             }
             dft_small<S, R>(xa);
-            dft_small<S, R>(xb);
+            if (NC == 2) dft_small<S, R>(xb);
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 const int row = j + r * NBR;
-                if (MODE != kColsAdj || s_rows[row >> a.tsh])
-                    st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+                if (MODE != kColsAdj || s_rows[row >> a.tsh]) {
+                    if (NC == 2) st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+                    else __stcg(col + (size_t)row * pitch, xa[r]);
+                }
             }
         }
     }
@@ -765,7 +779,7 @@ __global__ void k_twiddles(float2 *tw, int n)
     }
 }
 
-template <int N> size_t col_smem() { return (size_t)2 * col_stride<N>() * sizeof(float2); }
+template <int N> size_t col_smem() { return (size_t)kColsPerCta * col_stride<N>() * sizeof(float2); }
 template <int N> size_t row_smem(int planes, int ntu)
 {
     return ((FftPlan<N>::PAD * 8 + 15) / 16) * 16 + (size_t)4 * N * sizeof(float) +
@@ -779,7 +793,7 @@ cudaError_t run_cols(const ColArgs &a, int planes, cudaStream_t s)
     cudaError_t e = cudaFuncSetAttribute(k_cols<N, S, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_cols<N, S, MODE><<<dim3(a.nx / 2, planes), col_threads<N>(),
+    k_cols<N, S, MODE><<<dim3(a.nx / kColsPerCta, planes), col_threads<N>(),
                          smem, s>>>(a);
     return cudaGetLastError();
 }
