@@ -372,7 +372,7 @@ __device__ __forceinline__ void fft_row(float2 (&v)[N / T], float2 *buf, int t,
 
 enum { kColsFwd = 0, kColsAdj = 1, kColsPlain = 2 };
 
-template <int N> __host__ __device__ constexpr int fft_threads() { return N / 16 < 256 ? N / 16 : 256; }
+template <int N> __host__ __device__ constexpr int fft_threads() { return N / 16 < 512 ? N / 16 : 512; }
 template <int N> __host__ __device__ constexpr int col_group() { return 2; }
 // stride between the column buffers: congruent to 16/COLS modulo 16 so that
 // the transposing loads (COLS columns of consecutive rows) hit distinct banks
