@@ -106,7 +106,9 @@ typedef enum {
     WSG_ERR_NOMEM = 4,      /* device allocation failed                    */
     WSG_ERR_STATE = 5,      /* call out of order (e.g. adjoint before bin) */
     WSG_ERR_CAPACITY = 6,   /* more points than the reserved capacity      */
-    WSG_ERR_UNSUPPORTED = 7 /* configuration outside the kernels' limits   */
+    WSG_ERR_UNSUPPORTED = 7,/* configuration outside the kernels' limits   */
+    WSG_ERR_IO = 8          /* a file could not be opened, read or written
+                               (wstack_gb300_io.h)                         */
 } wsg_status;
 
 typedef enum {

@@ -9,6 +9,8 @@ The compute lives in ``libwstack_gb300.so`` (CUDA kernels behind a C ABI,
 * ``autograd``  ``torch.autograd.Function`` over the forward imaging operator
                 and its hand-written adjoint
 * ``synth``     seeded synthetic observations in the reference's input layout
+* ``binms``     the reference's parameter, meta and binary files, its dumps,
+                and its main() as ``run``
 * ``build``     the nvcc recipe that produces the shared library
 """
 from ._lib import WSG_FP32C, WSG_FP64, WstackError  # noqa: F401

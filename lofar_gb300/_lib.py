@@ -1,4 +1,5 @@
-"""ctypes binding of libwstack_gb300.so (the C ABI in include/wstack_gb300.h).
+"""ctypes binding of libwstack_gb300.so (the C ABI in include/wstack_gb300.h and
+include/wstack_gb300_io.h).
 
 The library is required: there is no CPU or pure-PyTorch fallback.  If it is
 missing, loading raises immediately with the command that builds it.
@@ -19,13 +20,14 @@ WSG_ERR_NOMEM = 4
 WSG_ERR_STATE = 5
 WSG_ERR_CAPACITY = 6
 WSG_ERR_UNSUPPORTED = 7
+WSG_ERR_IO = 8
 
 WSG_FP64 = 0
 WSG_FP32C = 1
 
 STATUS_NAMES = {0: "WSG_OK", 1: "WSG_ERR_ARG", 2: "WSG_ERR_CUDA", 3: "WSG_ERR_CUFFT",
                 4: "WSG_ERR_NOMEM", 5: "WSG_ERR_STATE", 6: "WSG_ERR_CAPACITY",
-                7: "WSG_ERR_UNSUPPORTED"}
+                7: "WSG_ERR_UNSUPPORTED", 8: "WSG_ERR_IO"}
 
 
 class WstackError(RuntimeError):
@@ -54,12 +56,52 @@ class Channel(ctypes.Structure):
                 ("vis_img", ctypes.c_void_p), ("weight", ctypes.c_void_p)]
 
 
+# include/wstack_gb300_io.h
+WSG_MAX_DATASETS = 100
+WSG_PATH_LEN = 1024
+WSG_NAME_LEN = 256
+WSG_DROPPED_ROWS = 1000
+
+PARAM_NAMES = ("ufile", "vfile", "wfile", "weightsfile", "visrealfile", "visimgfile", "metafile",
+               "outfile", "outfile1", "outfile2", "outfile3", "fftfile", "fftfile2", "fftfile3",
+               "logfile", "extension", "timingfile")
+
+
+class Params(ctypes.Structure):
+    _fields_ = ([(f, ctypes.c_int) for f in ("num_threads", "ndatasets", "grid_size_x",
+                                               "grid_size_y", "num_w_planes", "w_support",
+                                               "verbose_level", "n_datapaths")]
+                + [("datapath", (ctypes.c_char * WSG_PATH_LEN) * WSG_MAX_DATASETS)]
+                + [(f, ctypes.c_char * WSG_NAME_LEN) for f in PARAM_NAMES])
+
+
+class Metadata(ctypes.Structure):
+    _fields_ = [("Nmeasures", ctypes.c_long), ("Nvis", ctypes.c_long), ("Nweights", ctypes.c_long),
+                ("freq_per_chan", ctypes.c_long), ("polarisations", ctypes.c_long),
+                ("Ntimes", ctypes.c_long), ("dt", ctypes.c_double), ("thours", ctypes.c_double),
+                ("baselines", ctypes.c_long), ("uvmin", ctypes.c_double),
+                ("uvmax", ctypes.c_double), ("wmin", ctypes.c_double), ("wmax", ctypes.c_double)]
+
+
+class RunOptions(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("write_data", ctypes.c_int),
+                ("write_image", ctypes.c_int), ("write_timings", ctypes.c_int),
+                ("verbose", ctypes.c_int), ("outdir", ctypes.c_char * WSG_PATH_LEN)]
+
+
+class RunReport(ctypes.Structure):
+    _fields_ = [("datasets", ctypes.c_int), ("Nmeasures", ctypes.c_long), ("Nvis", ctypes.c_long),
+                ("resolution", ctypes.c_double), ("dropped", ctypes.c_longlong)] + \
+               [(f, ctypes.c_double) for f in ("setup", "compose", "kernel", "reduce", "fft",
+                                               "phase", "write", "total")]
+
+
 _P = ctypes.c_void_p
 _D = ctypes.c_double
 _I = ctypes.c_int
 _L = ctypes.c_long
 
-# name -> (restype, argtypes); every symbol of include/wstack_gb300.h
+# name -> (restype, argtypes); every symbol of include/*.h
 SIGNATURES = {
     "wstack": (None, [_I, _L, _L, _L, _P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P, _I]),
     "phase_correction": (None, [_P, _P, _P, _I, _I, _I, _I, _I, _D, _D, _D, _I]),
@@ -108,6 +150,20 @@ SIGNATURES = {
     "wsg_batch_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
     "wsg_batch_device_bytes": (ctypes.c_longlong, [_P]),
     "wsg_grid_noalloc": (_I, [_I, _L, _L, _L, _P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P, _P]),
+    # include/wstack_gb300_io.h
+    "wsg_read_parameter_file": (_I, [ctypes.c_char_p, ctypes.POINTER(Params)]),
+    "wsg_read_metadata": (_I, [ctypes.c_char_p, ctypes.POINTER(Metadata)]),
+    "wsg_partition_measurements": (_I, [ctypes.POINTER(Metadata), _I, _I, ctypes.POINTER(_L)]),
+    "wsg_read_measurements": (_I, [ctypes.POINTER(Params), _I, ctypes.POINTER(Metadata), _L,
+                                   _P, _P, _P, _P, _P, _P]),
+    "wsg_reference_resolution": (_I, [_D, _D, ctypes.POINTER(_D)]),
+    "wsg_write_cube_dump": (_I, [_P, _I, _I, _I, _D, ctypes.c_char_p, ctypes.c_char_p]),
+    "wsg_plan_dump_cube": (_I, [_P, _P, _D, ctypes.c_char_p, ctypes.c_char_p]),
+    "wsg_write_image_dump": (_I, [_P, _P, _L, ctypes.c_char_p, ctypes.c_char_p]),
+    "wsg_write_timings": (_I, [ctypes.c_char_p, ctypes.POINTER(_D)]),
+    "wsg_run_options_default": (None, [ctypes.POINTER(RunOptions)]),
+    "wsg_run_paramfile": (_I, [ctypes.c_char_p, ctypes.POINTER(RunOptions),
+                               ctypes.POINTER(RunReport)]),
 }
 
 _lib = None

@@ -19,7 +19,11 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwstack_gb300.so")
 
-SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "capi.cu", "batch.cu", "noalloc.cu"]
+SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "capi.cu", "batch.cu",
+           "noalloc.cu", "binms.cu", "driver.cu"]
+# the reference's executable (main.c) over the library: wstack_gb300_run PARAMFILE ...
+RUNNER_SRC = "wstack_run.cpp"
+RUNNER = os.path.join(HERE, "wstack_gb300_run")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -51,6 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     headers.append(os.path.join(INCLUDE, "wstack_gb300.h"))
+    headers.append(os.path.join(INCLUDE, "wstack_gb300_io.h"))
     headers.append(os.path.abspath(__file__))
     objs = []
     jobs = []
@@ -76,6 +81,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         link = [nvcc, *ARCH, "-shared", "-cudart", "shared", *objs, "-o", LIB,
                 f"-L{cuda_lib}", "-lcufft", "-Xlinker", f"-rpath={cuda_lib}"]
         run(link)
+    runner_src = os.path.join(CSRC, RUNNER_SRC)
+    if force or _stale(RUNNER, [runner_src, LIB, *headers]):
+        run(["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", runner_src, "-o", RUNNER, f"-L{HERE}",
+             "-lwstack_gb300", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -10,7 +10,12 @@ Two shared libraries are produced:
   It is built only when the reference tree is present; its sources are never
   copied into this repository.
 
-Both use the same flags (``-O2 -ffp-contract=off``) so that a single-threaded
+A third artefact, ``oracle/_ref/refio``, is the reference's own reader
+(``init.c`` + ``allvars.c``, compiled where they lie with ``-DUSE_MPI`` and the
+single-process stand-in header ``refshim/mpi.h``) driven by
+``refio_main.c``; it is also built only when the reference tree is present.
+
+The two shared libraries use the same flags (``-O2 -ffp-contract=off``) so that a single-threaded
 run of one is bit-identical to the other on x86-64 and aarch64.
 """
 from __future__ import annotations
@@ -25,6 +30,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SO = os.path.join(REF_DIR, "libref.so")
+REFIO = os.path.join(REF_DIR, "refio")
 REFERENCE_TREE = os.environ.get("WSTACK_REFERENCE_TREE", "/root/reference")
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"]
@@ -69,10 +75,31 @@ def build_ref(force: bool = False) -> str | None:
     return REF_SO
 
 
+def build_refio(force: bool = False) -> str | None:
+    """Compile the reference's reader (init.c, allvars.c) with refio_main.c, if present.
+
+    The reference compiles these files with -DUSE_MPI (Makefile:23); its
+    non-MPI branch of init.c does not compile (allocate_memory names
+    undeclared variables).  With one process every MPI call in them is a
+    broadcast or a barrier, which refshim/mpi.h turns into no-ops."""
+    srcs = [os.path.join(REFERENCE_TREE, f) for f in ("init.c", "allvars.c")]
+    if not all(os.path.exists(s) for s in srcs):
+        return REFIO if os.path.exists(REFIO) else None
+    main_c = os.path.join(HERE, "refio_main.c")
+    shim = os.path.join(HERE, "refshim", "mpi.h")
+    os.makedirs(REF_DIR, exist_ok=True)
+    if force or not _newer(REFIO, srcs + [main_c, shim, __file__]):
+        cmd = ["gcc", "-O1", "-fopenmp", "-DUSE_MPI", "-w", f"-I{os.path.join(HERE, 'refshim')}",
+               f"-I{REFERENCE_TREE}", main_c, *srcs, "-o", REFIO, "-lm"]
+        subprocess.run(cmd, check=True)
+    return REFIO
+
+
 def main() -> int:
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force))
+    print(build_refio(force))
     return 0
 
 

@@ -3,6 +3,7 @@
 No compute call is made here: these run without a GPU.
 """
 import ctypes
+import glob
 import os
 import re
 import subprocess
@@ -13,10 +14,11 @@ from lofar_gb300 import _lib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "wstack_gb300.h")
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
 def declared_symbols():
-    text = "\n".join(ln for ln in open(HEADER).read().splitlines()
+    text = "\n".join(ln for h in HEADERS for ln in open(h).read().splitlines()
                      if not ln.lstrip().startswith("#"))
     return sorted(set(re.findall(r"WSG_API\s+[\w\s\*]*?\b(\w+)\s*\(", text)))
 
