@@ -18,6 +18,9 @@ sample on this host's cores.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
     python bench.py --workload c4     # the (channel, polarisation) batch: 16 channels
                                       # x 4 polarisations, 2048^2 x 16 planes each
+    python bench.py --workload driver --steps 3   # the reference's main() on files:
+                                      # read a dataset directory, grid, FFT, w-correct,
+                                      # write the image dump (wsg_run_paramfile)
 
 Roofline traffic (DRAM bytes per launch of the gridding stage's kernels) is
 read from the committed ncu launch-list summary of the same workload
@@ -51,9 +54,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "driver"],
                     help="c2: one 4096^2 x 32 image (default); c4: the channel x pol batch; "
-                         "c5: one 8192^2 x 128 image, support 9, 400M visibilities")
+                         "c5: one 8192^2 x 128 image, support 9, 400M visibilities; "
+                         "driver: c2 as files through the reference's main()")
+    ap.add_argument("--driver-dir", default=None,
+                    help="driver: directory for the dataset and dump files (default: a temp dir)")
+    ap.add_argument("--driver-write-data", action="store_true",
+                    help="driver: also time one run with the grid and fft dumps")
     ap.add_argument("--subset", type=int, default=1_000_000,
                     help="c5: visibilities in the subset checked against the FP64 oracle")
     ap.add_argument("--window", type=int, default=512, help="c5: edge of the checked window")
@@ -782,6 +790,101 @@ def bench_large(args, rank, world, peak, peak_kind):
     }
 
 
+def bench_driver(args, rank, world, peak, peak_kind):
+    """The reference's main() on files (wsg_run_paramfile): the c2 observation
+    written as a reference dataset directory (meta.txt + six binary files, plus
+    the 1000 rows the reader drops), then per step: read, upload, bin, grid,
+    per-plane FFT, w-correct, download and write the image dump.  FP64 (the
+    reference's arithmetic) and FP32C.  Stage times are the driver's wall
+    clock; the files are in the page cache after the first read."""
+    import shutil
+    import tempfile
+
+    import torch
+    from lofar_gb300 import binms, synth
+    from oracle import binms_oracle as B
+
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    gen = dict(synth.CONFIGS["c2"]["gen"])
+    gen["n_vis"] = args.nvis
+    d = synth.observe_device(device="cuda", **gen)
+    n, nx, P, S = d["n"], args.nx, args.planes, args.support
+    tmp = tempfile.mkdtemp(prefix="wstack_driver_", dir=args.driver_dir)
+    try:
+        ds = os.path.join(tmp, "ds0") + "/"
+        pad = {"uu": 0.5, "vv": 0.5, "ww": 0.5, "weight": 1.0, "vis_real": 0.0, "vis_img": 0.0}
+        host = {}
+        for k, v in pad.items():
+            a = d[k].cpu().numpy()
+            host[k] = np.concatenate([a, np.full(1000, v, a.dtype)])
+        binms.write_dataset(ds, uu=host["uu"], vv=host["vv"], ww=host["ww"],
+                            weights=host["weight"], vis_real=host["vis_real"],
+                            vis_img=host["vis_img"], freq_per_chan=1, polarisations=1,
+                            uvmin=d["uvmin"], uvmax=d["uvmax"], wmin=d["wmin"], wmax=d["wmax"])
+        bytes_in = sum(os.path.getsize(os.path.join(ds, f)) for f in os.listdir(ds))
+        del host, d
+        torch.cuda.empty_cache()
+        pf = os.path.join(tmp, "paramfile.txt")
+        with open(pf, "w") as f:
+            f.write(f"ndatasets 1\nDatapath1 {ds}\nnum_threads 1\nw_support {S}\n"
+                    f"grid_size_x {nx}\ngrid_size_y {nx}\nnum_w_planes {P}\n"
+                    "ufile ucoord.bin\nvfile vcoord.bin\nwfile wcoord.bin\n"
+                    "weightsfile weights.bin\nvisrealfile visibilities_real.bin\n"
+                    "visimgfile visibilities_img.bin\nmetafile meta.txt\n"
+                    "outfile2 grid_real.bin\noutfile3 grid_img.bin\nfftfile2 fft_real.bin\n"
+                    "fftfile3 fft_img.bin\ntimingfile timings.dat\n")
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        res = {}
+        clocks = ClockSampler(dev)
+        clocks.start()
+        for prec in ("fp64", "fp32c"):
+            for _ in range(args.warmup):
+                binms.run(pf, write_image=True, precision=prec, outdir=out)
+            reps = [binms.run(pf, write_image=True, precision=prec, outdir=out)
+                    for _ in range(args.steps)]
+            med = {k: statistics.median(r[k] for r in reps)
+                   for k in ("setup", "compose", "kernel", "fft", "phase", "write", "total")}
+            res[prec] = {"mvis_s": n / med["total"] / 1e6, "stages_s": med,
+                         "read_GBps": bytes_in / med["setup"] / 1e9,
+                         "dropped": reps[-1]["dropped"]}
+        clk = clocks.stop()
+        if args.driver_write_data:
+            r = binms.run(pf, write_data=True, precision="fp32c", outdir=out)
+            cube = 2 * 2 * P * nx * nx * 8   # two dumps, two float64 files each
+            res["write_data_fp32c"] = {"write_s": r["write"], "dump_bytes": cube,
+                                       "dump_GBps": cube / r["write"] / 1e9,
+                                       "total_s": r["total"]}
+        # the oracle port of the reader on the same files (one thread)
+        t = time.perf_counter()
+        prm = B.parse_parameter_file(open(pf).read())
+        meta, start = B.partition(B.parse_metadata(open(ds + "meta.txt").read()))
+        B.read_measurements(ds, prm, meta, start)
+        cpu_read_s = time.perf_counter() - t
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    ms = max_over_ranks(res["fp64"]["stages_s"]["total"] * 1e3, world)
+    if rank != 0:
+        return None
+    return {
+        "metric": "Mvis/s files-to-image through the reference's main() (read + grid + FFT + "
+                  "w-correct + image dump)",
+        "value": whole_job_mvis(n, world, ms), "unit": "Mvis/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the c2 observation written as a reference dataset directory)",
+        "config": {"workload": f"wsg_run_paramfile: {nx}x{nx} grid, {P} w-planes, support {S}, "
+                               f"{n} measurements (+1000 dropped) from {bytes_in} bytes of files",
+                   "files": "page cache after the first read", "parallelism": f"replicas{world}"},
+        "precisions": res, "clocks": clk,
+        "cpu_baseline": {"value": cpu_read_s, "unit": "s to read the dataset", "cores": 1,
+                         "kind": "port", "sample": "the whole dataset through the NumPy reader "
+                                                   "restatement (oracle/binms_oracle.py)"},
+        "gpu_launches": None,
+    }
+
+
 def roofline(per, n, nx, P, sc, peak, peak_kind):
     ab = algorithmic_bytes(n, nx, nx, P, sc)
     med = {s: statistics.median(v) for s, v in per.items() if v}
@@ -816,8 +919,8 @@ def main():
 
     import torch
     peak, peak_kind = peaks()
-    if args.workload in ("c4", "c5"):
-        fn = bench_batch if args.workload == "c4" else bench_large
+    if args.workload in ("c4", "c5", "driver"):
+        fn = {"c4": bench_batch, "c5": bench_large, "driver": bench_driver}[args.workload]
         line = fn(args, rank, world, peak, peak_kind)
         if line is not None:
             print(json.dumps(line))

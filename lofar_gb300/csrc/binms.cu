@@ -3,13 +3,20 @@
 // dumps and timing line.  Declared in include/wstack_gb300_io.h, which lists
 // the formats and the reference lines each function replaces.
 //
-// Reading and writing are host work bounded by the file system; the device
-// part is wsg_plan_dump_cube, which splits a resident cube into real and
-// imaginary float64 planes on the GPU and overlaps the download of one chunk
-// with the file write of the previous one.
+// Reading and writing are host work bounded by the file system: the reader
+// cuts the six files into chunks read by a pool of threads, and each dump
+// writes its real and imaginary files from two threads.  The device part is
+// wsg_plan_dump_cube, which splits a resident cube into real and imaginary
+// float64 chunks on the GPU and overlaps the download of one chunk with the
+// file writes of the previous one.
 #include <cuda_runtime.h>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cerrno>
 #include <climits>
@@ -19,6 +26,7 @@
 #include <cstring>
 #include <future>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "plan.cuh"
@@ -87,8 +95,76 @@ std::string joined(const char *dir, const char *name)
 }
 
 // ---------------------------------------------------------------------------
+// parallel reader: every file is cut into chunks that a pool of threads reads
+// with pread, so the page cache (or the disk) is read with all cores; the
+// part of a buffer beyond the end of a short file is zero-filled
+// ---------------------------------------------------------------------------
+
+constexpr long long kReadChunk = 32ll << 20;
+
+struct ReadJob {
+    const char *what;            // the reference's word in its "error opening" messages
+    std::string path;
+    void *dst;
+    long long bytes;             // wanted
+    long long offset;            // in the file
+    int fd = -1;
+    std::atomic<bool> short_read{false};
+    ReadJob(const char *w, std::string p, void *d, long long b, long long o)
+        : what(w), path(std::move(p)), dst(d), bytes(b), offset(o) {}
+};
+
+void read_parallel(ReadJob *jobs, int njobs)
+{
+    struct Piece {
+        ReadJob *job;
+        long long from, len;     // bytes of the destination
+    };
+    std::vector<Piece> pieces;
+    for (int k = 0; k < njobs; ++k) {
+        ReadJob &j = jobs[k];
+        struct stat st;
+        long long avail = 0;
+        if (fstat(j.fd, &st) == 0) avail = std::max(0ll, (long long)st.st_size - j.offset);
+        if (avail < j.bytes) {
+            j.short_read = true;
+            memset(static_cast<char *>(j.dst) + avail, 0, (size_t)(j.bytes - avail));
+        }
+        const long long have = std::min(avail, j.bytes);
+        for (long long a = 0; a < have; a += kReadChunk)
+            pieces.push_back({&j, a, std::min(kReadChunk, have - a)});
+    }
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < pieces.size();) {
+            const Piece &pc = pieces[i];
+            char *dst = static_cast<char *>(pc.job->dst) + pc.from;
+            long long done = 0;
+            while (done < pc.len) {
+                const ssize_t r = pread(pc.job->fd, dst + done, (size_t)(pc.len - done),
+                                        (off_t)(pc.job->offset + pc.from + done));
+                if (r <= 0) {   // the file shrank or failed under us: zero the rest
+                    pc.job->short_read = true;
+                    memset(dst + done, 0, (size_t)(pc.len - done));
+                    break;
+                }
+                done += r;
+            }
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nthreads = std::min<size_t>(std::min(16u, hw), pieces.size());
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+    worker();
+    for (std::thread &t : pool) t.join();
+}
+
+// ---------------------------------------------------------------------------
 // device cube -> planar float64 chunks
 // ---------------------------------------------------------------------------
+
+constexpr long long kDumpChunk = 8ll << 20;   // values per chunk of a device dump
 
 template <typename C>
 __global__ void k_split_cube(const C *__restrict__ cube, double *__restrict__ re,
@@ -103,6 +179,21 @@ __global__ void k_split_cube(const C *__restrict__ cube, double *__restrict__ re
 }
 
 }  // namespace
+
+cudaError_t wsg::launch_split_complex(const void *src, int prec, double *re, double *im,
+                                      long long n, double scale, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((n + threads - 1) / threads, 152ll * 8);
+    if (prec == WSG_FP64)
+        k_split_cube<double2><<<blocks, threads, 0, stream>>>(static_cast<const double2 *>(src), re,
+                                                              im, n, scale);
+    else
+        k_split_cube<float2><<<blocks, threads, 0, stream>>>(static_cast<const float2 *>(src), re,
+                                                             im, n, scale);
+    return cudaGetLastError();
+}
 
 extern "C" {
 
@@ -251,48 +342,31 @@ int wsg_read_measurements(const wsg_params *prm, int dataset, const wsg_metadata
     if (m->Nmeasures > 0 && (!uu || !vv || !ww || !weights || !vis_real || !vis_img))
         return set_error(WSG_ERR_ARG, "NULL buffer");
     const char *dir = prm->datapath[dataset];
-
-    struct Job {
-        const char *what;      // the reference's word in its "error opening" messages
-        std::string path;
-        void *dst;
-        size_t elem;
-        long long count;
-        long long offset;      // bytes
-    };
     const long long pol = m->polarisations, fp = m->freq_per_chan * m->polarisations;
-    Job jobs[6] = {
-        {"ucoord", joined(dir, prm->ufile), uu, 8, m->Nmeasures, startrow * 8ll},
-        {"vcoord", joined(dir, prm->vfile), vv, 8, m->Nmeasures, startrow * 8ll},
-        {"wcoord", joined(dir, prm->wfile), ww, 8, m->Nmeasures, startrow * 8ll},
-        {"weights", joined(dir, prm->weightsfile), weights, 4, m->Nweights, startrow * pol * 4},
-        {"visibilities real", joined(dir, prm->visrealfile), vis_real, 4, m->Nvis, startrow * fp * 4},
-        {"visibilities img", joined(dir, prm->visimgfile), vis_img, 4, m->Nvis, startrow * fp * 4},
+    ReadJob jobs[6] = {
+        {"ucoord", joined(dir, prm->ufile), uu, 8ll * m->Nmeasures, startrow * 8ll},
+        {"vcoord", joined(dir, prm->vfile), vv, 8ll * m->Nmeasures, startrow * 8ll},
+        {"wcoord", joined(dir, prm->wfile), ww, 8ll * m->Nmeasures, startrow * 8ll},
+        {"weights", joined(dir, prm->weightsfile), weights, 4ll * m->Nweights, startrow * pol * 4},
+        {"visibilities real", joined(dir, prm->visrealfile), vis_real, 4ll * m->Nvis,
+         startrow * fp * 4},
+        {"visibilities img", joined(dir, prm->visimgfile), vis_img, 4ll * m->Nvis,
+         startrow * fp * 4},
     };
-    // 0 = read in full, 1 = cannot open, 2 = short
-    auto read_one = [](const Job &j) -> int {
-        File fp(j.path.c_str(), "rb");
-        if (!fp.f) return 1;
-        if (j.count <= 0) return 0;
-        size_t got = 0;
-        if (fseeko(fp.f, (off_t)j.offset, SEEK_SET) == 0)
-            got = fread(j.dst, j.elem, (size_t)j.count, fp.f);
-        if ((long long)got == j.count) return 0;
-        memset(static_cast<char *>(j.dst) + got * j.elem, 0, ((size_t)j.count - got) * j.elem);
-        return 2;
-    };
-    std::future<int> fut[6];
-    for (int k = 0; k < 6; ++k) fut[k] = std::async(std::launch::async, read_one, std::cref(jobs[k]));
-    int res[6];
-    for (int k = 0; k < 6; ++k) res[k] = fut[k].get();
-    for (int k = 0; k < 6; ++k)
-        if (res[k] == 1)
-            return set_error(WSG_ERR_IO, "error opening %s file %s", jobs[k].what,
-                             jobs[k].path.c_str());
-    for (int k = 0; k < 6; ++k)
-        if (res[k] == 2)
-            return set_error(WSG_ERR_IO, "an error occurred while reading file %s",
-                             jobs[k].path.c_str());
+    // open in the reference's order: the first file that cannot be opened is reported
+    for (ReadJob &j : jobs) {
+        j.fd = open(j.path.c_str(), O_RDONLY);
+        if (j.fd < 0) {
+            for (ReadJob &k : jobs)
+                if (k.fd >= 0) close(k.fd);
+            return set_error(WSG_ERR_IO, "error opening %s file %s", j.what, j.path.c_str());
+        }
+    }
+    read_parallel(jobs, 6);
+    for (ReadJob &j : jobs) close(j.fd);
+    for (const ReadJob &j : jobs)
+        if (j.short_read.load())
+            return set_error(WSG_ERR_IO, "an error occurred while reading file %s", j.path.c_str());
     return WSG_OK;
 }
 
@@ -319,19 +393,21 @@ int wsg_write_cube_dump(const double *cube, int planes, int ny, int nx, double s
     if (!fr.f) return set_error(WSG_ERR_IO, "cannot open %s for writing", real_path);
     if (!fi.f) return set_error(WSG_ERR_IO, "cannot open %s for writing", img_path);
     const long long n = (long long)planes * ny * nx;
-    const long long chunk = 1ll << 20;
-    std::vector<double> re((size_t)(n < chunk ? n : chunk)), im(re.size());
-    for (long long i0 = 0; i0 < n; i0 += chunk) {
-        const long long c = n - i0 < chunk ? n - i0 : chunk;
-        for (long long i = 0; i < c; ++i) {
-            re[i] = cube[2 * (i0 + i)] * scale;
-            im[i] = cube[2 * (i0 + i) + 1] * scale;
+    // one thread per file: each takes its component of the interleaved cube
+    auto write_part = [&](int part, FILE *f) -> bool {
+        const long long chunk = 1ll << 20;
+        std::vector<double> buf((size_t)std::min(n, chunk));
+        for (long long i0 = 0; i0 < n; i0 += chunk) {
+            const long long c = std::min(n - i0, chunk);
+            for (long long i = 0; i < c; ++i) buf[i] = cube[2 * (i0 + i) + part] * scale;
+            if (fwrite(buf.data(), sizeof(double), (size_t)c, f) != (size_t)c) return false;
         }
-        if (fwrite(re.data(), sizeof(double), (size_t)c, fr.f) != (size_t)c)
-            return set_error(WSG_ERR_IO, "write to %s failed", real_path);
-        if (fwrite(im.data(), sizeof(double), (size_t)c, fi.f) != (size_t)c)
-            return set_error(WSG_ERR_IO, "write to %s failed", img_path);
-    }
+        return true;
+    };
+    auto im_ok = std::async(std::launch::async, write_part, 1, fi.f);
+    const bool re_ok = write_part(0, fr.f);
+    if (!im_ok.get()) return set_error(WSG_ERR_IO, "write to %s failed", img_path);
+    if (!re_ok) return set_error(WSG_ERR_IO, "write to %s failed", real_path);
     if (!fr.close()) return set_error(WSG_ERR_IO, "closing %s failed", real_path);
     if (!fi.close()) return set_error(WSG_ERR_IO, "closing %s failed", img_path);
     return WSG_OK;
@@ -347,77 +423,52 @@ int wsg_plan_dump_cube(wsg_plan *p, const void *cube, double scale, const char *
     if (!fi.f) return set_error(WSG_ERR_IO, "cannot open %s for writing", img_path);
 
     const long long n = p->cube_planes() * p->npix();
-    const long long chunk = n < (8ll << 20) ? n : (8ll << 20);   // 128 MiB of float64 pairs
+    const long long chunk = std::min(n, kDumpChunk);
     DevBuf stage;
     WSG_CUDA(stage.ensure(2 * 2 * (size_t)chunk * sizeof(double)));
-    double *host = nullptr;
-    WSG_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&host), 2 * 2 * (size_t)chunk * sizeof(double),
-                           cudaHostAllocDefault));
-    cudaEvent_t done[2] = {nullptr, nullptr};
-    // writer[b] appends the chunk held in slot b; each writer first waits for
-    // the one before it, so chunks reach the files in order
-    std::shared_future<int> writer[2];
-    int status = WSG_OK;
-    const int threads = 256;
-    const int blocks = (int)std::min<long long>((chunk + threads - 1) / threads, 152ll * 8);
-
-    // the writer of slot b: wait for its download, append both halves
-    auto write_slot = [&](int b, long long c) -> int {
-        if (cudaEventSynchronize(done[b]) != cudaSuccess) return WSG_ERR_CUDA;
-        const double *re = host + (size_t)b * 2 * chunk;
-        const double *im = re + chunk;
-        if (fwrite(re, sizeof(double), (size_t)c, fr.f) != (size_t)c) return WSG_ERR_IO;
-        if (fwrite(im, sizeof(double), (size_t)c, fi.f) != (size_t)c) return WSG_ERR_IO;
-        return WSG_OK;
+    // two slots of (re, im) host staging; each file has its own chain of
+    // writers, and each writer waits for the one before it on the same file,
+    // so chunks reach the files in order while the next chunk is split and
+    // downloaded
+    std::vector<double> host[2];
+    std::shared_future<bool> wre[2], wim[2];
+    auto chain = [](std::shared_future<bool> prev, FILE *f, const double *src, long long c) {
+        return std::async(std::launch::async, [prev, f, src, c]() {
+                   if (prev.valid() && !prev.get()) return false;
+                   return fwrite(src, sizeof(double), (size_t)c, f) == (size_t)c;
+               }).share();
     };
-
+    bool ok = true;
     cudaError_t e = cudaSuccess;
-    for (int b = 0; b < 2 && e == cudaSuccess; ++b)
-        e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
-    for (long long i0 = 0, k = 0; e == cudaSuccess && status == WSG_OK && i0 < n; i0 += chunk, ++k) {
+    for (long long i0 = 0, k = 0; ok && e == cudaSuccess && i0 < n; i0 += chunk, ++k) {
         const int b = (int)(k & 1);
-        const long long c = n - i0 < chunk ? n - i0 : chunk;
-        if (writer[b].valid()) status = writer[b].get();   // slot b's previous chunk is on disk
-        if (status != WSG_OK) break;
+        const long long c = std::min(n - i0, chunk);
+        if (wre[b].valid()) ok = wre[b].get() && ok;   // slot b's last chunk is written
+        if (wim[b].valid()) ok = wim[b].get() && ok;
+        if (!ok) break;
         double *dre = stage.as<double>() + (size_t)b * 2 * chunk;
         double *dim = dre + chunk;
-        if (p->prec == WSG_FP64)
-            k_split_cube<double2><<<blocks, threads, 0, p->stream>>>(
-                static_cast<const double2 *>(cube) + i0, dre, dim, c, scale);
-        else
-            k_split_cube<float2><<<blocks, threads, 0, p->stream>>>(
-                static_cast<const float2 *>(cube) + i0, dre, dim, c, scale);
-        e = cudaGetLastError();
-        double *hre = host + (size_t)b * 2 * chunk;
+        e = launch_split_complex(static_cast<const char *>(cube) + (size_t)i0 * p->elem(), p->prec,
+                                 dre, dim, c, scale, p->stream);
+        if (host[b].empty()) host[b].resize(2 * (size_t)chunk);
+        double *hre = host[b].data(), *him = hre + chunk;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(hre, dre, (size_t)c * sizeof(double), cudaMemcpyDeviceToHost, p->stream);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(hre + chunk, dim, (size_t)c * sizeof(double), cudaMemcpyDeviceToHost,
-                                p->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(done[b], p->stream);
+            e = cudaMemcpyAsync(him, dim, (size_t)c * sizeof(double), cudaMemcpyDeviceToHost, p->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
         if (e == cudaSuccess) {
-            std::shared_future<int> prev = writer[b ^ 1];
-            writer[b] = std::async(std::launch::async, [&write_slot, prev, b, c]() {
-                            if (prev.valid()) {
-                                const int s = prev.get();
-                                if (s != WSG_OK) return s;
-                            }
-                            return write_slot(b, c);
-                        }).share();
+            wre[b] = chain(wre[b ^ 1], fr.f, hre, c);
+            wim[b] = chain(wim[b ^ 1], fi.f, him, c);
         }
     }
-    for (int b = 0; b < 2; ++b)
-        if (writer[b].valid()) {
-            int s = writer[b].get();
-            if (status == WSG_OK) status = s;
-        }
-    for (int b = 0; b < 2; ++b)
-        if (done[b]) cudaEventDestroy(done[b]);
-    cudaFreeHost(host);
+    for (int b = 0; b < 2; ++b) {
+        if (wre[b].valid()) ok = wre[b].get() && ok;
+        if (wim[b].valid()) ok = wim[b].get() && ok;
+    }
     if (e != cudaSuccess)
         return set_error(WSG_ERR_CUDA, "wsg_plan_dump_cube: %s", cudaGetErrorString(e));
-    if (status == WSG_ERR_CUDA) return set_error(WSG_ERR_CUDA, "wsg_plan_dump_cube: download failed");
-    if (status != WSG_OK) return set_error(WSG_ERR_IO, "write to %s / %s failed", real_path, img_path);
+    if (!ok) return set_error(WSG_ERR_IO, "write to %s / %s failed", real_path, img_path);
     if (!fr.close()) return set_error(WSG_ERR_IO, "closing %s failed", real_path);
     if (!fi.close()) return set_error(WSG_ERR_IO, "closing %s failed", img_path);
     return WSG_OK;
@@ -433,10 +484,12 @@ int wsg_write_image_dump(const double *image_real, const double *image_imag, lon
     File fr(real_path, "wb"), fi(img_path, "wb");
     if (!fr.f) return set_error(WSG_ERR_IO, "cannot open %s for writing", real_path);
     if (!fi.f) return set_error(WSG_ERR_IO, "cannot open %s for writing", img_path);
-    if (fwrite(image_real, sizeof(double), (size_t)npix, fr.f) != (size_t)npix)
-        return set_error(WSG_ERR_IO, "write to %s failed", real_path);
-    if (fwrite(image_imag, sizeof(double), (size_t)npix, fi.f) != (size_t)npix)
-        return set_error(WSG_ERR_IO, "write to %s failed", img_path);
+    auto im_ok = std::async(std::launch::async, [&]() {
+        return fwrite(image_imag, sizeof(double), (size_t)npix, fi.f) == (size_t)npix;
+    });
+    const bool re_ok = fwrite(image_real, sizeof(double), (size_t)npix, fr.f) == (size_t)npix;
+    if (!im_ok.get()) return set_error(WSG_ERR_IO, "write to %s failed", img_path);
+    if (!re_ok) return set_error(WSG_ERR_IO, "write to %s failed", real_path);
     if (!fr.close()) return set_error(WSG_ERR_IO, "closing %s failed", real_path);
     if (!fi.close()) return set_error(WSG_ERR_IO, "closing %s failed", img_path);
     return WSG_OK;

@@ -346,7 +346,9 @@ int wsg_plan_reserve(wsg_plan *p, long max_points)
         return set_error(WSG_ERR_UNSUPPORTED, "max_points outside [0, 1e9]");
     WSG_TRY(ensure_records(p, max_points));
     WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->cube_planes() * p->npix()));
-    WSG_TRY(ensure_fft(p));
+    // the FP32C power-of-two grids transform with the library's own kernels
+    WSG_TRY(p->fused ? ensure_fused(p) : ensure_fft(p));
+    if (p->wc_set) WSG_TRY(ensure_wscreen(p));
     return WSG_OK;
 }
 

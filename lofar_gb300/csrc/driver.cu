@@ -22,7 +22,10 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "plan.cuh"
 #include "wstack_gb300_io.h"
@@ -36,12 +39,6 @@ double now_s()
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-struct HostDeleter {
-    void operator()(void *p) const
-    {
-        if (p) cudaFreeHost(p);
-    }
-};
 struct DevDeleter {
     void operator()(void *p) const
     {
@@ -60,16 +57,7 @@ struct StreamDeleter {
         if (s) cudaStreamDestroy(s);
     }
 };
-using HostPtr = std::unique_ptr<void, HostDeleter>;
 using DevPtr = std::unique_ptr<void, DevDeleter>;
-
-int host_alloc(HostPtr &out, size_t bytes)
-{
-    void *p = nullptr;
-    WSG_CUDA(cudaHostAlloc(&p, bytes ? bytes : 16, cudaHostAllocDefault));
-    out.reset(p);
-    return WSG_OK;
-}
 
 int dev_alloc(DevPtr &out, size_t bytes)
 {
@@ -111,13 +99,44 @@ long keep_slab_rows(long n, long nf, long np, double *uu, double *vv, double *ww
     return k;
 }
 
-int run_dataset(const wsg_params &prm, int index, const wsg_run_options &o, cudaStream_t stream,
-                wsg_run_report &rep)
+// The device side of one dataset, prepared on a second host thread while the
+// files are read: the plan with its records, resident grid and FFT plan, the
+// input buffers and the image buffers.
+struct DeviceSide {
+    std::unique_ptr<wsg_plan, PlanDeleter> plan;
+    DevPtr in[6];          // uu, vv, ww, weights, vis_real, vis_img
+    DevPtr image, split;   // complex image; its real and imaginary float64 planes
+    int status = WSG_OK;
+    std::string message;
+};
+
+int prepare_device(DeviceSide &d, const wsg_params &prm, const wsg_metadata &meta,
+                   double resolution, const wsg_run_options &o, cudaStream_t stream)
+{
+    const int nx = prm.grid_size_x, ny = prm.grid_size_y, planes = prm.num_w_planes;
+    wsg_plan *raw = nullptr;
+    WSG_TRY(wsg_plan_create(&raw, nx, ny, planes, prm.w_support, 1.0 / (double)nx,
+                            1.0 / (double)planes, o.precision, stream));
+    d.plan.reset(raw);
+    WSG_TRY(wsg_plan_set_wcorrection(raw, resolution, meta.wmin, meta.wmax));
+    WSG_TRY(wsg_plan_reserve(raw, meta.Nmeasures));
+    const size_t b_uvw = sizeof(double) * meta.Nmeasures, b_wt = sizeof(float) * meta.Nweights,
+                 b_vis = sizeof(float) * meta.Nvis;
+    const size_t bytes[6] = {b_uvw, b_uvw, b_uvw, b_wt, b_vis, b_vis};
+    for (int k = 0; k < 6; ++k) WSG_TRY(dev_alloc(d.in[k], bytes[k]));
+    const size_t npix = (size_t)nx * ny;
+    WSG_TRY(dev_alloc(d.image, (o.precision == WSG_FP64 ? 16 : 8) * npix));
+    WSG_TRY(dev_alloc(d.split, 2 * sizeof(double) * npix));
+    return WSG_OK;
+}
+
+int run_dataset(const wsg_params &prm, int index, const wsg_run_options &o, int device,
+                cudaStream_t stream, wsg_run_report &rep)
 {
     const double t_start = now_s();
     if (o.verbose) printf("\nDataset %d\n", index);
 
-    // ---- init: meta file, partition, binary files ----------------------------
+    // ---- init: meta file, partition ------------------------------------------
     wsg_metadata meta;
     const std::string metapath = std::string(prm.datapath[index]) + prm.metafile;
     WSG_TRY(wsg_read_metadata(metapath.c_str(), &meta));
@@ -127,79 +146,72 @@ int run_dataset(const wsg_params &prm, int index, const wsg_run_options &o, cuda
     if (o.verbose) {
         printf("N. measurements %ld\n", meta.Nmeasures);
         printf("N. visibilities %ld\n", meta.Nvis);
-        printf("READING DATA\n");
     }
-    const long n = meta.Nmeasures, nf = meta.freq_per_chan, np = meta.polarisations;
-    HostPtr h_uu, h_vv, h_ww, h_wt, h_vr, h_vi;
-    WSG_TRY(host_alloc(h_uu, sizeof(double) * n));
-    WSG_TRY(host_alloc(h_vv, sizeof(double) * n));
-    WSG_TRY(host_alloc(h_ww, sizeof(double) * n));
-    WSG_TRY(host_alloc(h_wt, sizeof(float) * meta.Nweights));
-    WSG_TRY(host_alloc(h_vr, sizeof(float) * meta.Nvis));
-    WSG_TRY(host_alloc(h_vi, sizeof(float) * meta.Nvis));
-    int st = wsg_read_measurements(&prm, index, &meta, startrow, (double *)h_uu.get(),
-                                   (double *)h_vv.get(), (double *)h_ww.get(), (float *)h_wt.get(),
-                                   (float *)h_vr.get(), (float *)h_vi.get());
-    if (st != WSG_OK) {
-        // a short file: the reference prints and carries on with zeros
-        if (st != WSG_ERR_IO || strncmp(wstack_gb300_last_error_string(), "an error occurred", 17))
-            return st;
-        fprintf(stderr, "%s\n", wstack_gb300_last_error_string());
-        clear_error();
-    }
-    const long rows = keep_slab_rows(n, nf, np, (double *)h_uu.get(), (double *)h_vv.get(),
-                                     (double *)h_ww.get(), (float *)h_wt.get(), (float *)h_vr.get(),
-                                     (float *)h_vi.get());
     double resolution = 0.0;
     WSG_TRY(wsg_reference_resolution(meta.uvmin, meta.uvmax, &resolution));
+    const long n = meta.Nmeasures, nf = meta.freq_per_chan, np = meta.polarisations;
+
+    // ---- the device side on a second thread, the binary files on this one -----
+    DeviceSide dev;
+    std::thread prep([&]() {
+        cudaSetDevice(device);
+        dev.status = prepare_device(dev, prm, meta, resolution, o, stream);
+        if (dev.status != WSG_OK) dev.message = wstack_gb300_last_error_string();
+    });
+    if (o.verbose) printf("READING DATA\n");
+    // pageable buffers: no pinning cost, and first-touched by the reader threads
+    const size_t bytes[6] = {sizeof(double) * n, sizeof(double) * n, sizeof(double) * n,
+                             sizeof(float) * meta.Nweights, sizeof(float) * meta.Nvis,
+                             sizeof(float) * meta.Nvis};
+    std::unique_ptr<unsigned char[]> host[6];
+    for (int k = 0; k < 6; ++k) host[k].reset(new (std::nothrow) unsigned char[bytes[k] ? bytes[k] : 1]);
+    int st = WSG_OK;
+    for (int k = 0; k < 6; ++k)
+        if (!host[k]) st = set_error(WSG_ERR_NOMEM, "host buffer of %zu bytes", bytes[k]);
+    if (st == WSG_OK) {
+        st = wsg_read_measurements(&prm, index, &meta, startrow, (double *)host[0].get(),
+                                   (double *)host[1].get(), (double *)host[2].get(),
+                                   (float *)host[3].get(), (float *)host[4].get(),
+                                   (float *)host[5].get());
+        if (st == WSG_ERR_IO && !strncmp(wstack_gb300_last_error_string(), "an error occurred", 17)) {
+            // a short file: the reference prints and carries on with zeros
+            fprintf(stderr, "%s\n", wstack_gb300_last_error_string());
+            clear_error();
+            st = WSG_OK;
+        }
+    }
+    prep.join();
+    if (st != WSG_OK) return st;
+    if (dev.status != WSG_OK) return set_error(dev.status, "%s", dev.message.c_str());
+    double *h_uu = (double *)host[0].get(), *h_vv = (double *)host[1].get(),
+           *h_ww = (double *)host[2].get();
+    float *h_wt = (float *)host[3].get(), *h_vr = (float *)host[4].get(),
+          *h_vi = (float *)host[5].get();
+    const long rows = keep_slab_rows(n, nf, np, h_uu, h_vv, h_ww, h_wt, h_vr, h_vi);
     const double t_setup = now_s();
 
     // ---- gridding ------------------------------------------------------------
-    const int nx = prm.grid_size_x, ny = prm.grid_size_y, planes = prm.num_w_planes;
+    const int nx = prm.grid_size_x, ny = prm.grid_size_y;
     if (o.verbose)
         printf("RESOLUTION = %f rad, %f arcsec\n", resolution,
                resolution * (3600.0 * 180.0) / 3.14159265359);
-    wsg_plan *raw = nullptr;
-    WSG_TRY(wsg_plan_create(&raw, nx, ny, planes, prm.w_support, 1.0 / (double)nx,
-                            1.0 / (double)planes, o.precision, stream));
-    std::unique_ptr<wsg_plan, PlanDeleter> plan(raw);
-    WSG_TRY(wsg_plan_set_wcorrection(plan.get(), resolution, meta.wmin, meta.wmax));
-    DevPtr d_uu, d_vv, d_ww, d_wt, d_vr, d_vi;
-    const size_t b_uvw = sizeof(double) * rows, b_wt = sizeof(float) * rows * np,
-                 b_vis = sizeof(float) * rows * nf * np;
-    WSG_TRY(dev_alloc(d_uu, b_uvw));
-    WSG_TRY(dev_alloc(d_vv, b_uvw));
-    WSG_TRY(dev_alloc(d_ww, b_uvw));
-    WSG_TRY(dev_alloc(d_wt, b_wt));
-    WSG_TRY(dev_alloc(d_vr, b_vis));
-    WSG_TRY(dev_alloc(d_vi, b_vis));
-    if (rows > 0) {
-        WSG_CUDA(cudaMemcpyAsync(d_uu.get(), h_uu.get(), b_uvw, cudaMemcpyHostToDevice, stream));
-        WSG_CUDA(cudaMemcpyAsync(d_vv.get(), h_vv.get(), b_uvw, cudaMemcpyHostToDevice, stream));
-        WSG_CUDA(cudaMemcpyAsync(d_ww.get(), h_ww.get(), b_uvw, cudaMemcpyHostToDevice, stream));
-        WSG_CUDA(cudaMemcpyAsync(d_wt.get(), h_wt.get(), b_wt, cudaMemcpyHostToDevice, stream));
-        WSG_CUDA(cudaMemcpyAsync(d_vr.get(), h_vr.get(), b_vis, cudaMemcpyHostToDevice, stream));
-        WSG_CUDA(cudaMemcpyAsync(d_vi.get(), h_vi.get(), b_vis, cudaMemcpyHostToDevice, stream));
-    }
-    WSG_TRY(wsg_bin(plan.get(), rows, nf, np, (const double *)d_uu.get(), (const double *)d_vv.get(),
-                    (const double *)d_ww.get(), (const float *)d_vr.get(),
-                    (const float *)d_vi.get(), (const float *)d_wt.get()));
+    wsg_plan *plan = dev.plan.get();
+    const size_t rbytes[6] = {sizeof(double) * rows, sizeof(double) * rows, sizeof(double) * rows,
+                              sizeof(float) * rows * np, sizeof(float) * rows * nf * np,
+                              sizeof(float) * rows * nf * np};
+    for (int k = 0; k < 6 && rows > 0; ++k)
+        WSG_CUDA(cudaMemcpyAsync(dev.in[k].get(), host[k].get(), rbytes[k], cudaMemcpyHostToDevice,
+                                 stream));
+    WSG_TRY(wsg_bin(plan, rows, nf, np, (const double *)dev.in[0].get(),
+                    (const double *)dev.in[1].get(), (const double *)dev.in[2].get(),
+                    (const float *)dev.in[4].get(), (const float *)dev.in[5].get(),
+                    (const float *)dev.in[3].get()));
     WSG_CUDA(cudaStreamSynchronize(stream));
     const double t_compose = now_s();
-    // the measurements are binned into the plan's records: free the raw inputs
-    d_uu.reset();
-    d_vv.reset();
-    d_ww.reset();
-    d_wt.reset();
-    d_vr.reset();
-    d_vi.reset();
-
-    const size_t elem = o.precision == WSG_FP64 ? 2 * sizeof(double) : 2 * sizeof(float);
-    const long long npix = (long long)nx * ny;
-    DevPtr d_cube, d_image;
-    WSG_TRY(dev_alloc(d_cube, elem * (size_t)planes * npix));
-    WSG_TRY(dev_alloc(d_image, elem * (size_t)npix));
-    WSG_TRY(wsg_grid(plan.get(), d_cube.get()));
+    // the inputs are now binned into the plan's records; their buffers are
+    // released with the dataset (a cudaFree here would wait for the device)
+    void *cube = wsg_plan_grid(plan);
+    WSG_TRY(wsg_grid(plan, cube));
     WSG_CUDA(cudaStreamSynchronize(stream));
     const double t_kernel = now_s();
     double t_write = 0.0;
@@ -207,47 +219,49 @@ int run_dataset(const wsg_params &prm, int index, const wsg_run_options &o, cuda
     if (o.write_data) {
         if (o.verbose) printf("WRITING GRIDDED DATA\n");
         const double t0 = now_s();
-        WSG_TRY(wsg_plan_dump_cube(plan.get(), d_cube.get(), 1.0,
-                                   out_path(o, index, prm.outfile2).c_str(),
+        WSG_TRY(wsg_plan_dump_cube(plan, cube, 1.0, out_path(o, index, prm.outfile2).c_str(),
                                    out_path(o, index, prm.outfile3).c_str()));
         t_write += now_s() - t0;
     }
 
     // ---- fft + phase correction -----------------------------------------------
     if (o.verbose) printf("PERFORMING FFT\n");
+    const long long npix = (long long)nx * ny;
     const double scale = 1.0 / (double)npix;
-    double t_fft0 = now_s(), t_fft = 0.0, t_phase0 = 0.0;
-    if (o.write_data) {
-        WSG_TRY(wsg_fft(plan.get(), d_cube.get(), +1));
+    const double t_fft0 = now_s();
+    double t_fft = 0.0, t_phase0 = 0.0;
+    if (o.write_data || o.precision == WSG_FP64) {
+        WSG_TRY(wsg_fft(plan, cube, +1));
         WSG_CUDA(cudaStreamSynchronize(stream));
         t_fft = now_s() - t_fft0;
-        if (o.verbose) printf("WRITING FFT TRANSFORMED DATA\n");
-        const double t0 = now_s();
-        WSG_TRY(wsg_plan_dump_cube(plan.get(), d_cube.get(), scale,
-                                   out_path(o, index, prm.fftfile2).c_str(),
-                                   out_path(o, index, prm.fftfile3).c_str()));
-        t_write += now_s() - t0;
+        if (o.write_data) {
+            if (o.verbose) printf("WRITING FFT TRANSFORMED DATA\n");
+            const double t0 = now_s();
+            WSG_TRY(wsg_plan_dump_cube(plan, cube, scale, out_path(o, index, prm.fftfile2).c_str(),
+                                       out_path(o, index, prm.fftfile3).c_str()));
+            t_write += now_s() - t0;
+        }
         if (o.verbose) printf("PHASE CORRECTION\n");
         t_phase0 = now_s();
-        WSG_TRY(wsg_wcorrect(plan.get(), d_cube.get(), d_image.get(), scale));
-    } else if (o.precision == WSG_FP64) {
-        WSG_TRY(wsg_fft(plan.get(), d_cube.get(), +1));
-        WSG_CUDA(cudaStreamSynchronize(stream));
-        t_fft = now_s() - t_fft0;
-        if (o.verbose) printf("PHASE CORRECTION\n");
-        t_phase0 = now_s();
-        WSG_TRY(wsg_wcorrect(plan.get(), d_cube.get(), d_image.get(), scale));
+        WSG_TRY(wsg_wcorrect(plan, cube, dev.image.get(), scale));
     } else {
         // one fused launch transforms each plane and applies the w-correction
-        WSG_TRY(wsg_fft_wcorrect(plan.get(), d_cube.get(), d_image.get(), 1));
+        WSG_TRY(wsg_fft_wcorrect(plan, cube, dev.image.get(), 1));
         WSG_CUDA(cudaStreamSynchronize(stream));
         t_fft = now_s() - t_fft0;
         if (o.verbose) printf("PHASE CORRECTION\n");
         t_phase0 = now_s();
     }
-    HostPtr h_img, h_re, h_im;
-    WSG_TRY(host_alloc(h_img, elem * (size_t)npix));
-    WSG_CUDA(cudaMemcpyAsync(h_img.get(), d_image.get(), elem * (size_t)npix, cudaMemcpyDeviceToHost,
+    // image_real / image_imag in host memory, as the reference's phase_correction
+    // leaves them (fourier_transform.c:170-173)
+    std::unique_ptr<double[]> image_re(new (std::nothrow) double[npix]),
+        image_im(new (std::nothrow) double[npix]);   // not zero-filled: the download writes all
+    if (!image_re || !image_im) return set_error(WSG_ERR_NOMEM, "host image of %lld pixels", npix);
+    double *d_re = (double *)dev.split.get(), *d_im = d_re + npix;
+    WSG_CUDA(launch_split_complex(dev.image.get(), o.precision, d_re, d_im, npix, 1.0, stream));
+    WSG_CUDA(cudaMemcpyAsync(image_re.get(), d_re, sizeof(double) * npix, cudaMemcpyDeviceToHost,
+                             stream));
+    WSG_CUDA(cudaMemcpyAsync(image_im.get(), d_im, sizeof(double) * npix, cudaMemcpyDeviceToHost,
                              stream));
     WSG_CUDA(cudaStreamSynchronize(stream));
     const double t_phase = now_s() - t_phase0;
@@ -255,35 +269,20 @@ int run_dataset(const wsg_params &prm, int index, const wsg_run_options &o, cuda
     if (o.write_image) {
         if (o.verbose) printf("WRITING IMAGE\n");
         const double t0 = now_s();
-        WSG_TRY(host_alloc(h_re, sizeof(double) * (size_t)npix));
-        WSG_TRY(host_alloc(h_im, sizeof(double) * (size_t)npix));
-        double *re = (double *)h_re.get(), *im = (double *)h_im.get();
-        if (o.precision == WSG_FP64) {
-            const double *z = (const double *)h_img.get();
-            for (long long i = 0; i < npix; ++i) {
-                re[i] = z[2 * i];
-                im[i] = z[2 * i + 1];
-            }
-        } else {
-            const float *z = (const float *)h_img.get();
-            for (long long i = 0; i < npix; ++i) {
-                re[i] = (double)z[2 * i];
-                im[i] = (double)z[2 * i + 1];
-            }
-        }
-        WSG_TRY(wsg_write_image_dump(re, im, (long)npix, out_path(o, index, prm.fftfile2).c_str(),
+        WSG_TRY(wsg_write_image_dump(image_re.get(), image_im.get(), (long)npix,
+                                     out_path(o, index, prm.fftfile2).c_str(),
                                      out_path(o, index, prm.fftfile3).c_str()));
         t_write += now_s() - t0;
     }
 
     wsg_stats stats;
-    WSG_TRY(wsg_plan_get_stats(plan.get(), &stats));
+    WSG_TRY(wsg_plan_get_stats(plan, &stats));
     const double total = now_s() - t_start;
     const double setup = t_setup - t_start, compose = t_compose - t_setup,
                  kernel = t_kernel - t_compose;
     if (o.write_timings) {
-        const double s[7] = {setup, kernel, compose, 0.0, t_fft, t_phase, total};
-        WSG_TRY(wsg_write_timings(out_path(o, index, prm.timingfile).c_str(), s));
+        const double sec[7] = {setup, kernel, compose, 0.0, t_fft, t_phase, total};
+        WSG_TRY(wsg_write_timings(out_path(o, index, prm.timingfile).c_str(), sec));
     }
     if (o.verbose) {
         printf("%14s time : %f sec\n", "Setup", setup);
@@ -347,11 +346,13 @@ int wsg_run_paramfile(const char *paramfile, const wsg_run_options *opt, wsg_run
     if (prm->grid_size_x <= 0 || prm->grid_size_y <= 0 || prm->num_w_planes <= 0)
         return set_error(WSG_ERR_ARG, "grid_size_x, grid_size_y and num_w_planes must be positive");
 
+    int device = 0;
+    WSG_CUDA(cudaGetDevice(&device));
     cudaStream_t s = nullptr;
     WSG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     std::unique_ptr<CUstream_st, StreamDeleter> stream(s);
     for (int i = 0; i < prm->ndatasets; ++i) {
-        const int st = run_dataset(*prm, i, o, s, rep);
+        const int st = run_dataset(*prm, i, o, device, s, rep);
         if (report) *report = rep;
         if (st != WSG_OK) return st;
     }

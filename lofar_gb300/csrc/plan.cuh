@@ -65,6 +65,11 @@ struct DevBuf {
     template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
 };
 
+// src: n complex values (complex128 when prec == WSG_FP64, else complex64) ->
+// re[i] = scale * real, im[i] = scale * imag as float64 (binms.cu).
+cudaError_t launch_split_complex(const void *src, int prec, double *re, double *im, long long n,
+                                 double scale, cudaStream_t stream);
+
 // d == 2^-k exactly (0 <= k <= 1000).
 bool is_pow2_recip(double d, int &k);
 // ptr is device (or managed) memory of the current context.
