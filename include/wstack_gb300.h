@@ -307,6 +307,51 @@ WSG_API int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per_ch
                              const float *weight, double dx, double dw, int w_support,
                              int grid_size_x, int grid_size_y, double *grid, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* 4. v-slab sectoring (the reference's multi-rank decomposition)      */
+/* ------------------------------------------------------------------ */
+
+/*
+ * A rank of the reference grids its rows slab by slab: nsectors v-slabs of
+ * yaxis grid rows each (nsectors = ranks, yaxis = grid_size_y / nsectors,
+ * init.c:24-33).  Row i belongs to slab b = (int)(vv[i]*nsectors), and also
+ * to slab b+1 (b-1) when its distance to that slab's edge is below
+ * w_supporth = ((w_support-1)/2)*dx (init.c:18), computed exactly as
+ * gridding.c:45-55 does.  Each slab's list holds its rows in increasing
+ * order; histo_send has nsectors+1 entries (the last slab, b == nsectors, is
+ * never gridded).  Rows whose slab index would fall outside [0, nsectors]
+ * (the reference indexes histo_send out of bounds for them) fail the call with
+ * WSG_ERR_ARG.  Limits: nsectors <= WSG_MAX_SECTORS, n <= 1e9.
+ */
+#define WSG_MAX_SECTORS 1023
+
+/* Slab list offsets only: offsets[s] = first entry of slab s, offsets[nsectors+1]
+   = total entries (histo_send[s] = offsets[s+1] - offsets[s]).  vv and offsets
+   are device memory; returns after the work on `stream` has finished. */
+WSG_API int wsg_sector_count(const double *vv, long n, long nsectors, int yaxis, double dx,
+                             double w_supporth, long *offsets, void *stream);
+/* Offsets and the concatenated lists: index[offsets[s] .. offsets[s+1]) is
+   sectorarray[s] (gridding.c:58-77).  Device memory; capacity = entries of
+   index (at most 3*n are needed), WSG_ERR_CAPACITY when too small. */
+WSG_API int wsg_sector_lists(const double *vv, long n, long nsectors, int yaxis, double dx,
+                             double w_supporth, long *offsets, long *index, long capacity,
+                             void *stream);
+/* The composition step of gridding_data() (gridding.c:193-211) for slab
+   isector on the device: list = that slab's nsec entries of index; writes
+   the slab's rows in reverse list order with vvs = vv - isector*(dx*yaxis),
+   ready for wstack() on a yaxis-row grid.  Asynchronous on `stream`. */
+WSG_API int wsg_sector_gather(const long *list, long nsec, long isector, int yaxis, double dx,
+                              long freq_per_chan, long polarisations, const double *uu,
+                              const double *vv, const double *ww, const float *weights,
+                              const float *vis_real, const float *vis_img, double *uus,
+                              double *vvs, double *wws, float *weightss, float *visreals,
+                              float *visimgs, void *stream);
+/* Drop-in for initialize_array() (gridding.c:35-86): vv in host or device
+   memory; fills histo_send[nsectors+1] and sectorarray[nsectors+1] in host
+   memory, each list allocated with malloc() (free() it), on the GPU. */
+WSG_API int wsg_initialize_array(const double *vv, long n, long nsectors, int yaxis, double dx,
+                                 double w_supporth, long *histo_send, long **sectorarray);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,7 @@ WSG_MAX_DATASETS = 100
 WSG_PATH_LEN = 1024
 WSG_NAME_LEN = 256
 WSG_DROPPED_ROWS = 1000
+WSG_MAX_SECTORS = 1023
 
 PARAM_NAMES = ("ufile", "vfile", "wfile", "weightsfile", "visrealfile", "visimgfile", "metafile",
                "outfile", "outfile1", "outfile2", "outfile3", "fftfile", "fftfile2", "fftfile3",
@@ -150,6 +151,11 @@ SIGNATURES = {
     "wsg_batch_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
     "wsg_batch_device_bytes": (ctypes.c_longlong, [_P]),
     "wsg_grid_noalloc": (_I, [_I, _L, _L, _L, _P, _P, _P, _P, _P, _P, _D, _D, _I, _I, _I, _P, _P]),
+    "wsg_sector_count": (_I, [_P, _L, _L, _I, _D, _D, _P, _P]),
+    "wsg_sector_lists": (_I, [_P, _L, _L, _I, _D, _D, _P, _P, _L, _P]),
+    "wsg_sector_gather": (_I, [_P, _L, _L, _I, _D, _L, _L, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                               _P, _P, _P, _P]),
+    "wsg_initialize_array": (_I, [_P, _L, _L, _I, _D, _D, _P, ctypes.POINTER(_P)]),
     # include/wstack_gb300_io.h
     "wsg_read_parameter_file": (_I, [ctypes.c_char_p, ctypes.POINTER(Params)]),
     "wsg_read_metadata": (_I, [ctypes.c_char_p, ctypes.POINTER(Metadata)]),

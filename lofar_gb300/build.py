@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwstack_gb300.so")
 
 SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "capi.cu", "batch.cu",
-           "noalloc.cu", "binms.cu", "driver.cu"]
+           "noalloc.cu", "binms.cu", "driver.cu", "sector.cu"]
 # the reference's executable (main.c) over the library: wstack_gb300_run PARAMFILE ...
 RUNNER_SRC = "wstack_run.cpp"
 RUNNER = os.path.join(HERE, "wstack_gb300_run")

@@ -125,14 +125,60 @@ def timings_line(seconds) -> str:
     return "%f %f %f %f %f %f %f\n" % tuple(seconds)
 
 
+def initialize_array(vv: np.ndarray, nsectors: int, yaxis: int, dx: float,
+                     w_supporth: float) -> tuple[np.ndarray, list]:
+    """gridding.c:35-86: histo_send[nsectors+1] and the per-slab row lists.
+
+    binphi = (int)(vv*nsectors); a row also joins slab binphi+1 (binphi-1)
+    when its distance to that edge, (double)((binphi+1)*yaxis)*dx - vv
+    (vv - (double)(binphi*yaxis)*dx), is in [0, w_supporth) (and binphi > 0
+    for the lower edge).  Lists are in increasing row order (the second pass
+    appends in row order).  NumPy float64 arithmetic is IEEE with one rounding
+    per operation, as the reference's C."""
+    vv = np.asarray(vv, dtype=np.float64)
+    x = vv * float(nsectors)
+    if not np.all((x > -1.0) & (x < nsectors + 1.0)):
+        raise ValueError("a row's slab index is outside [0, nsectors]")
+    b = np.trunc(x).astype(np.int64)
+    updist = ((b + 1) * yaxis).astype(np.float64) * dx - vv
+    downdist = vv - (b * yaxis).astype(np.float64) * dx
+    up = (updist < w_supporth) & (updist >= 0.0)
+    down = (downdist < w_supporth) & (b > 0) & (downdist >= 0.0)
+    if np.any(up & (b + 1 > nsectors)):
+        raise ValueError("a row joins slab nsectors + 1")
+    rows = np.arange(vv.shape[0], dtype=np.int64)
+    # (slab, row) pairs of every membership, ordered by slab then row
+    keys = np.concatenate([b, b[up] + 1, b[down] - 1])
+    who = np.concatenate([rows, rows[up], rows[down]])
+    order = np.lexsort((who, keys))
+    histo = np.bincount(keys, minlength=nsectors + 1).astype(np.int64)
+    lists = np.split(who[order], np.cumsum(histo)[:-1])
+    return histo, lists
+
+
+def sector_compose(lst: np.ndarray, isector: int, yaxis: int, dx: float, uu, vv, ww, weights,
+                   vis_real, vis_img, nf: int, npol: int) -> dict:
+    """gridding.c:193-211: the slab's rows in reverse list order, vv shifted
+    by isector*shift with shift = (double)(dx*yaxis)."""
+    r = np.asarray(lst, dtype=np.int64)[::-1]
+    shift = dx * float(yaxis)
+    return {"uu": np.asarray(uu)[r], "vv": np.asarray(vv)[r] - float(isector) * shift,
+            "ww": np.asarray(ww)[r],
+            "weights": np.asarray(weights).reshape(-1, npol)[r].reshape(-1),
+            "vis_real": np.asarray(vis_real).reshape(-1, nf * npol)[r].reshape(-1),
+            "vis_img": np.asarray(vis_img).reshape(-1, nf * npol)[r].reshape(-1)}
+
+
 def run_refio(paramfile: str, dataset: int, rank: int, size: int, outdir: str,
-              cwd: str | None = None) -> dict | None:
-    """Run the reference's reader (oracle/_ref/refio); None when it is not built."""
+              cwd: str | None = None, grid: bool = False) -> dict | None:
+    """Run the reference's reader and sectoring (oracle/_ref/refio), and with
+    ``grid`` its single-rank gridding and grid dump; None when it is not built."""
     if not os.path.exists(REFIO):
         return None
     os.makedirs(outdir, exist_ok=True)
-    r = subprocess.run([REFIO, paramfile, str(dataset), str(rank), str(size), outdir],
-                       capture_output=True, text=True, cwd=cwd)
+    outdir = os.path.abspath(outdir)
+    cmd = [REFIO, paramfile, str(dataset), str(rank), str(size), outdir] + (["grid"] if grid else [])
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=cwd)
     if r.returncode != 0:
         return {"returncode": r.returncode, "stdout": r.stdout, "stderr": r.stderr}
     params = {}
@@ -148,5 +194,9 @@ def run_refio(paramfile: str, dataset: int, rank: int, size: int, outdir: str,
         ("uu", "uu.bin", np.float64), ("vv", "vv.bin", np.float64), ("ww", "ww.bin", np.float64),
         ("weights", "weights.bin", np.float32), ("vis_real", "visreal.bin", np.float32),
         ("vis_img", "visimg.bin", np.float32))}
+    histo = np.array([int(x) for x in open(os.path.join(outdir, "histo.txt")).read().split()],
+                     dtype=np.int64)
+    flat = np.fromfile(os.path.join(outdir, "sectors.bin"), dtype=np.int64)
+    lists = np.split(flat, np.cumsum(histo)[:-1]) if histo.size else []
     return {"returncode": 0, "stdout": r.stdout, "params": params, "meta": meta,
-            "arrays": arrays}
+            "arrays": arrays, "histo": histo, "lists": lists, "outdir": outdir}

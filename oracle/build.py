@@ -10,8 +10,10 @@ Two shared libraries are produced:
   It is built only when the reference tree is present; its sources are never
   copied into this repository.
 
-A third artefact, ``oracle/_ref/refio``, is the reference's own reader
-(``init.c`` + ``allvars.c``, compiled where they lie with ``-DUSE_MPI`` and the
+A third artefact, ``oracle/_ref/refio``, is the reference's own reader,
+v-slab sectoring, single-rank gridding loop and grid dump writer
+(``init.c``, ``allvars.c``, ``gridding.c`` and ``w-stacking.cu`` as C,
+compiled where they lie with ``-DUSE_MPI -DWRITE_DATA`` and the
 single-process stand-in header ``refshim/mpi.h``) driven by
 ``refio_main.c``; it is also built only when the reference tree is present.
 
@@ -82,15 +84,19 @@ def build_refio(force: bool = False) -> str | None:
     non-MPI branch of init.c does not compile (allocate_memory names
     undeclared variables).  With one process every MPI call in them is a
     broadcast or a barrier, which refshim/mpi.h turns into no-ops."""
-    srcs = [os.path.join(REFERENCE_TREE, f) for f in ("init.c", "allvars.c")]
-    if not all(os.path.exists(s) for s in srcs):
+    srcs = [os.path.join(REFERENCE_TREE, f) for f in ("init.c", "allvars.c", "gridding.c")]
+    wstack_src = os.path.join(REFERENCE_TREE, "w-stacking.cu")
+    if not all(os.path.exists(s) for s in srcs + [wstack_src]):
         return REFIO if os.path.exists(REFIO) else None
     main_c = os.path.join(HERE, "refio_main.c")
     shim = os.path.join(HERE, "refshim", "mpi.h")
     os.makedirs(REF_DIR, exist_ok=True)
-    if force or not _newer(REFIO, srcs + [main_c, shim, __file__]):
-        cmd = ["gcc", "-O1", "-fopenmp", "-DUSE_MPI", "-w", f"-I{os.path.join(HERE, 'refshim')}",
-               f"-I{REFERENCE_TREE}", main_c, *srcs, "-o", REFIO, "-lm"]
+    if force or not _newer(REFIO, srcs + [wstack_src, main_c, shim, __file__]):
+        # -ffp-contract=off as for libref.so: the gridding sums are then the
+        # reference's exact operations on both host architectures
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-DUSE_MPI", "-DWRITE_DATA", "-w",
+               f"-I{os.path.join(HERE, 'refshim')}", f"-I{REFERENCE_TREE}", main_c, *srcs,
+               "-x", "c", wstack_src, "-x", "none", "-o", REFIO, "-lm"]
         subprocess.run(cmd, check=True)
     return REFIO
 

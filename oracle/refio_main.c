@@ -1,17 +1,24 @@
 /*
  * refio: runs the reference's own reader (init.c: read_parameter_file,
  * op_filename, readMetaData, metaData_calculation, allocate_memory, readData)
- * for one dataset and one rank, and writes what it read to an output
- * directory.  Test infrastructure only: it pins the library's reader
- * (wsg_read_parameter_file & co.) and the NumPy restatement in
- * oracle/binms_oracle.py against the reference itself.
+ * and v-slab sectoring (gridding.c: initialize_array) for one dataset and one
+ * rank, and writes what they produced to an output directory.  With the
+ * extra argument "grid" (one rank only) it then runs the reference's
+ * gridding loop and grid dump writer (gridding.c: gridding_data,
+ * write_gridded_data, compiled with WRITE_DATA) into the same directory.
+ * Test infrastructure only: it pins the library's reader, sectoring and dump
+ * writer, and the restatements in oracle/, against the reference itself.
  *
- *   refio PARAMFILE DATASET RANK SIZE OUTDIR
+ *   refio PARAMFILE DATASET RANK SIZE OUTDIR [grid]
  *
  * OUTDIR receives:
  *   params.txt   one "key value" line per parameter and output name
  *   meta.txt     the 13 meta fields after metaData_calculation, then startrow
  *   uu.bin vv.bin ww.bin weights.bin visreal.bin visimg.bin   as read
+ *   histo.txt    histo_send[0..nsectors] of initialize_array, nsectors = SIZE
+ *   sectors.bin  sectorarray[0..nsectors] concatenated, int64
+ *   with "grid": the grid dump files under the parameter file's outfile2 and
+ *   outfile3 names (prefixed with the dataset index, as the reference does)
  * The reference's steps run in init()'s order (init.c:10-65); the parameter
  * and meta files are read as rank 0 (which reads them and broadcasts), the
  * partition and the binary files as rank RANK of SIZE.
@@ -31,17 +38,27 @@ static void dump(const char *dir, const char *name, const void *p, size_t elem, 
 
 int main(int argc, char **argv)
 {
-    if (argc != 6) {
-        fprintf(stderr, "usage: refio PARAMFILE DATASET RANK SIZE OUTDIR\n");
+    if (argc != 6 && !(argc == 7 && !strcmp(argv[6], "grid"))) {
+        fprintf(stderr, "usage: refio PARAMFILE DATASET RANK SIZE OUTDIR [grid]\n");
         return 2;
     }
+    const int grid_mode = argc == 7;
     const int index = atoi(argv[2]), rank = atoi(argv[3]);
     const char *outdir = argv[5];
     size = atoi(argv[4]);
+    if (grid_mode && size != 1) {
+        fprintf(stderr, "refio: grid mode runs one rank\n");
+        return 2;
+    }
     global_rank = 0;
     read_parameter_file(argv[1]);
+    /* init.c:16-33 */
+    dx = 1.0 / (double)param.grid_size_x;
+    dw = 1.0 / (double)param.num_w_planes;
+    w_supporth = (double)((param.w_support - 1) / 2) * dx;
+    nsectors = size;
     xaxis = param.grid_size_x;
-    yaxis = param.grid_size_y / size;
+    yaxis = param.grid_size_y / nsectors;
     strcpy(datapath, param.datapath_multi[index]);
     sprintf(num_buf, "%d", index);
     op_filename();
@@ -86,5 +103,26 @@ int main(int argc, char **argv)
     dump(outdir, "weights.bin", data.weights, sizeof(float), metaData.Nweights);
     dump(outdir, "visreal.bin", data.visreal, sizeof(float), metaData.Nvis);
     dump(outdir, "visimg.bin", data.visimg, sizeof(float), metaData.Nvis);
+
+    initialize_array();
+    snprintf(path, sizeof(path), "%s/histo.txt", outdir);
+    f = fopen(path, "w");
+    if (!f) { perror(path); return 2; }
+    for (long s = 0; s <= nsectors; ++s) fprintf(f, "%ld\n", histo_send[s]);
+    fclose(f);
+    snprintf(path, sizeof(path), "%s/sectors.bin", outdir);
+    f = fopen(path, "wb");
+    if (!f) { perror(path); return 2; }
+    for (long s = 0; s <= nsectors; ++s)
+        if (histo_send[s] > 0) fwrite(sectorarray[s], sizeof(long), (size_t)histo_send[s], f);
+    fclose(f);
+
+    if (grid_mode) {
+        /* gridding() = initialize_array() + gridding_data() (gridding.c:8-33);
+           the lists were built above */
+        gridding_data();
+        if (chdir(outdir) != 0) { perror(outdir); return 2; }
+        write_gridded_data();
+    }
     return 0;
 }

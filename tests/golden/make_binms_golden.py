@@ -7,12 +7,17 @@ Run from anywhere in the container that holds the reference tree:
 
 1. Seeded small datasets in the reference's input layout (ds0: 1137 rows with
    2 channels x 2 polarisations; ds1: 1050 rows, 1 x 1; short: value files cut
-   short) and parameter files that exercise the reference's parsing rules.
-2. oracle/_ref/refio (the reference's init.c + allvars.c) reads each
-   (parameter file, dataset, rank, size) case; its parameters, meta values
-   after the partition, startrow and a SHA-256 of every array it read go to
-   expected.json.  tests/test_binms.py checks the library's reader against
-   expected.json, so the check needs neither the reference nor refio.
+   short; edges: rows on and around v-slab edges) and parameter files that
+   exercise the reference's parsing rules.
+2. oracle/_ref/refio (the reference's init.c, allvars.c and gridding.c) reads
+   each (parameter file, dataset, rank, size) case and sectors the rank's rows
+   into nsectors = size v-slabs; its parameters, meta values after the
+   partition, startrow, a SHA-256 of every array it read, histo_send and a
+   SHA-256 of the concatenated slab lists go to expected.json.
+3. One single-rank case runs the reference's gridding loop and grid dump
+   writer too; the two dump files are kept in ref_grid/.
+tests/test_binms.py checks the library and the restatements against these
+records, so the checks need neither the reference nor refio.
 """
 from __future__ import annotations
 
@@ -73,6 +78,28 @@ timingfile t.dat verbose_level 7 extension
 PARAMFILE_SHORT = PARAMFILE.replace("ndatasets              2", "ndatasets              1") \
                            .replace("ds0/", "short/")
 
+# one rank, one thread (a deterministic sum), a 32 x 32 x 4 grid
+PARAMFILE_GRID = PARAMFILE.replace("ndatasets              2", "ndatasets              1") \
+                          .replace("num_threads            2", "num_threads            1") \
+                          .replace("grid_size_x            64", "grid_size_x            32") \
+                          .replace("grid_size_y            64", "grid_size_y            32")
+
+PARAMFILE_EDGES = PARAMFILE.replace("ndatasets              2", "ndatasets              1") \
+                           .replace("ds0/", "edges/")
+
+
+def edge_rows():
+    """v values on, just inside and just outside the slab edges and the
+    w_supporth bands of a 64-row grid split into 1, 2, 4 and 8 slabs
+    (w_support 7: w_supporth = 3/64)."""
+    v = [0.0, 5e-324, 0.25, 0.5, 0.75, np.nextafter(1.0, 0.0)]
+    for k in range(1, 8):
+        e = k / 8.0
+        for d in (0.0, 3 / 64, -3 / 64, 2 / 64, -2 / 64):
+            x = e + d
+            v += [x, np.nextafter(x, 0.0), np.nextafter(x, 1.0)]
+    return np.array([x for x in v if 0.0 <= x < 1.0], dtype=np.float64)
+
 
 def _dataset(directory, n, nf, npol, seed, meta_text_fn, cut=None):
     rng = np.random.default_rng(seed)
@@ -117,14 +144,25 @@ def main() -> int:
              lambda n, nf, p: f"{n}\n{n * nf * p}\n{nf}\n{p}\n0\n1.0\n1.0\n1\n-100.0\n100.0\n"
                               f"-10.0\n10.0\n",
              cut={"visibilities_real.bin": 30 * 2 * 4, "visibilities_img.bin": 30 * 2 * 4})
+    ev = edge_rows()
+    _dataset(os.path.join(OUT, "edges"), len(ev) + 1000, 1, 1, 14,
+             lambda n, nf, p: f"{n}\n{n * nf * p}\n{nf}\n{p}\n0\n1.0\n1.0\n1\n-100.0\n"
+                              f"100.0\n-10.0\n10.0\n")
+    vfull = np.fromfile(os.path.join(OUT, "edges", "vcoord.bin"))
+    vfull[:len(ev)] = ev
+    vfull.tofile(os.path.join(OUT, "edges", "vcoord.bin"))
     for name, text in (("paramfile.txt", PARAMFILE), ("paramfile_quirks.txt", PARAMFILE_QUIRKS),
-                       ("paramfile_short.txt", PARAMFILE_SHORT)):
+                       ("paramfile_short.txt", PARAMFILE_SHORT),
+                       ("paramfile_grid.txt", PARAMFILE_GRID),
+                       ("paramfile_edges.txt", PARAMFILE_EDGES)):
         with open(os.path.join(OUT, name), "w") as f:
             f.write(text)
 
     cases = [("paramfile.txt", 0, 0, 1), ("paramfile.txt", 0, 0, 3), ("paramfile.txt", 0, 1, 3),
              ("paramfile.txt", 0, 2, 3), ("paramfile.txt", 1, 0, 1), ("paramfile.txt", 1, 1, 2),
+             ("paramfile.txt", 0, 3, 7), ("paramfile.txt", 0, 6, 7),
              ("paramfile_quirks.txt", 0, 0, 1), ("paramfile_short.txt", 0, 0, 1)]
+    cases += [("paramfile_edges.txt", 0, r, sz) for sz in (1, 2, 4, 8) for r in range(sz)]
     expected = []
     with tempfile.TemporaryDirectory() as tmp:
         for k, (pf, ds, rank, size) in enumerate(cases):
@@ -137,7 +175,21 @@ def main() -> int:
                 "params": r["params"], "meta": r["meta"],
                 "sha256": {k2: _sha(v) for k2, v in r["arrays"].items()},
                 "short_read": "an error occurred while reading file" in r["stdout"],
+                "histo": [int(x) for x in r["histo"]],
+                "sectors_sha256": _sha(np.concatenate(r["lists"]) if r["lists"] else
+                                       np.zeros(0, np.int64)),
             })
+        # the reference's single-rank gridding and grid dump
+        r = B.run_refio("paramfile_grid.txt", 0, 0, 1, os.path.join(tmp, "grid"), cwd=OUT,
+                        grid=True)
+        if r is None or r["returncode"] != 0:
+            print(f"refio grid failed: {r}", file=sys.stderr)
+            return 1
+        os.makedirs(os.path.join(OUT, "ref_grid"), exist_ok=True)
+        for f in ("0grid_real.bin", "0grid_img.bin"):
+            with open(os.path.join(r["outdir"], f), "rb") as src, \
+                    open(os.path.join(OUT, "ref_grid", f), "wb") as dst:
+                dst.write(src.read())
     with open(os.path.join(OUT, "expected.json"), "w") as f:
         json.dump(expected, f, indent=1, sort_keys=True)
     print(f"wrote {len(expected)} cases to {os.path.join(OUT, 'expected.json')}")

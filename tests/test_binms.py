@@ -133,6 +133,57 @@ def test_restatement_matches_the_reference_reader(case, monkeypatch):
             assert _sha(got[k]) == case["sha256"][k], k
 
 
+def _case_rows(case):
+    """The rows the case's rank reads, through the restatement."""
+    p = B.parse_parameter_file(open(os.path.join(GOLD, case["paramfile"])).read())
+    d = os.path.join(GOLD, p["datapath"][case["dataset"]])
+    meta, start = B.partition(B.parse_metadata(open(os.path.join(d, p["metafile"])).read()),
+                              case["rank"], case["size"])
+    return p, B.read_measurements(d + "/", p, meta, start)
+
+
+def _sector_geometry(p, size):
+    dx = 1.0 / p["grid_size_x"]
+    return size, p["grid_size_y"] // size, dx, float((p["w_support"] - 1) // 2) * dx
+
+
+@pytest.mark.parametrize("case", [c for c in EXPECTED if not c["short_read"]],
+                         ids=[i for i, c in zip(CASE_IDS, EXPECTED) if not c["short_read"]])
+def test_sector_restatement_matches_the_reference(case):
+    """initialize_array (gridding.c:35-86) restated, against the reference's
+    histo_send and lists for nsectors = ranks, edge rows included."""
+    p, rows = _case_rows(case)
+    histo, lists = B.initialize_array(rows["vv"], *_sector_geometry(p, case["size"]))
+    assert histo.tolist() == case["histo"]
+    assert _sha(np.concatenate(lists)) == case["sectors_sha256"]
+
+
+def test_reference_grid_dump_pins_the_oracle_and_the_writer(lib, tmp_path):
+    """The reference's own single-rank gridding and grid dump (ref_grid/,
+    num_threads 1) equal, bit for bit, the oracle gridding the slab's rows in
+    the reference's order (reverse list order) and the library's writer
+    dumping that grid."""
+    from oracle import oracle as O
+    p = B.parse_parameter_file(open(os.path.join(GOLD, "paramfile_grid.txt")).read())
+    d = os.path.join(GOLD, p["datapath"][0])
+    meta, start = B.partition(B.parse_metadata(open(os.path.join(d, p["metafile"])).read()))
+    rows = B.read_measurements(d, p, meta, start)
+    nx, ny, P, S = p["grid_size_x"], p["grid_size_y"], p["num_w_planes"], p["w_support"]
+    nf, npol = meta["freq_per_chan"], meta["polarisations"]
+    histo, lists = B.initialize_array(rows["vv"], *_sector_geometry(p, 1))
+    c = B.sector_compose(lists[0], 0, ny, 1.0 / nx, rows["uu"], rows["vv"], rows["ww"],
+                         rows["weights"], rows["vis_real"], rows["vis_img"], nf, npol)
+    grid = O.wstack(c["uu"], c["vv"], c["ww"], c["vis_real"], c["vis_img"], c["weights"],
+                    num_w_planes=P, freq_per_chan=nf, polarizations=npol, dx=1.0 / nx,
+                    dw=1.0 / P, w_support=S, nx=nx, ny=ny, num_threads=1)
+    ref_re = open(os.path.join(GOLD, "ref_grid", "0grid_real.bin"), "rb").read()
+    ref_im = open(os.path.join(GOLD, "ref_grid", "0grid_img.bin"), "rb").read()
+    cube = grid[..., 0] + 1j * grid[..., 1]
+    binms.write_cube_dump(cube, tmp_path / "re.bin", tmp_path / "im.bin")
+    assert (tmp_path / "re.bin").read_bytes() == ref_re
+    assert (tmp_path / "im.bin").read_bytes() == ref_im
+
+
 @pytest.mark.skipif(not os.path.exists(B.REFIO), reason="oracle/_ref/refio not built here")
 @pytest.mark.parametrize("case", EXPECTED, ids=CASE_IDS)
 def test_fixtures_still_match_a_fresh_reference_run(case, tmp_path):
@@ -143,6 +194,16 @@ def test_fixtures_still_match_a_fresh_reference_run(case, tmp_path):
     assert r["meta"] == case["meta"]
     for k in ARRAYS:
         assert _sha(r["arrays"][k]) == case["sha256"][k]
+    assert r["histo"].tolist() == case["histo"]
+    assert _sha(np.concatenate(r["lists"])) == case["sectors_sha256"]
+
+
+@pytest.mark.skipif(not os.path.exists(B.REFIO), reason="oracle/_ref/refio not built here")
+def test_reference_grid_fixture_still_matches_a_fresh_run(tmp_path):
+    r = B.run_refio("paramfile_grid.txt", 0, 0, 1, str(tmp_path), cwd=GOLD, grid=True)
+    assert r["returncode"] == 0
+    for f in ("0grid_real.bin", "0grid_img.bin"):
+        assert (tmp_path / f).read_bytes() == open(os.path.join(GOLD, "ref_grid", f), "rb").read()
 
 
 def test_python_front_end_reads_a_dataset(lib, monkeypatch):
@@ -304,6 +365,21 @@ def test_driver_argument_errors(lib, tmp_path):
         binms.run(tmp_path / "p.txt")
     with pytest.raises(WstackError, match="invalid precision"):
         binms.run(tmp_path / "p.txt", precision=5)
+
+
+def test_sector_argument_errors_need_no_gpu(lib):
+    assert lib.wsg_sector_count(None, 10, 0, 8, 1 / 64, 3 / 64, None, None) == \
+        _lib.WSG_ERR_UNSUPPORTED
+    assert lib.wsg_sector_count(None, 10, 1024, 8, 1 / 64, 3 / 64, None, None) == \
+        _lib.WSG_ERR_UNSUPPORTED
+    assert lib.wsg_sector_lists(None, 10, 4, 0, 1 / 64, 3 / 64, None, None, 0, None) == \
+        _lib.WSG_ERR_ARG
+    assert lib.wsg_sector_lists(None, 10, 4, 16, -1.0, 3 / 64, None, None, 0, None) == \
+        _lib.WSG_ERR_ARG
+    assert lib.wsg_sector_gather(None, 5, 0, 16, 1 / 64, 1, 1, *([None] * 12), None) == \
+        _lib.WSG_ERR_ARG
+    assert lib.wsg_initialize_array(None, 10, 4, 16, 1 / 64, 3 / 64, None, None) == \
+        _lib.WSG_ERR_ARG
 
 
 def test_runner_executable_usage(lib):
