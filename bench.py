@@ -790,6 +790,34 @@ def bench_large(args, rank, world, peak, peak_kind):
     }
 
 
+def bench_sectoring(vv, ny, support, reps=5):
+    """v-slab lists of the reference's multi-rank decomposition (wsg_sector_count
+    + wsg_sector_lists) on the device rows, for 16 and 256 slabs: median ms and
+    algorithmic GB/s (vv read once, the list entries and offsets written)."""
+    import torch
+    from lofar_gb300 import sectors
+    out = {}
+    for S in (16, 256):
+        yaxis, dx = ny // S, 1.0 / ny
+        wsh = sectors.w_supporth(support, dx)
+        times, entries = [], 0
+        for _ in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record()
+            _, off, index = sectors.sector_lists(vv, S, yaxis, dx, wsh)
+            b.record()
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+            entries = int(off[-1])
+            del index
+        ms = statistics.median(times[1:])
+        nbytes = 8 * vv.numel() + 8 * entries + 8 * (S + 2)
+        out[f"{S}_slabs"] = {"ms": ms, "entries": entries, "GBps": nbytes / ms / 1e6,
+                             "note": "count + lists calls, each with its own scan and host sync"}
+    return out
+
+
 def bench_driver(args, rank, world, peak, peak_kind):
     """The reference's main() on files (wsg_run_paramfile): the c2 observation
     written as a reference dataset directory (meta.txt + six binary files, plus
@@ -823,7 +851,9 @@ def bench_driver(args, rank, world, peak, peak_kind):
                             vis_img=host["vis_img"], freq_per_chan=1, polarisations=1,
                             uvmin=d["uvmin"], uvmax=d["uvmax"], wmin=d["wmin"], wmax=d["wmax"])
         bytes_in = sum(os.path.getsize(os.path.join(ds, f)) for f in os.listdir(ds))
-        del host, d
+        del host
+        sectoring = bench_sectoring(d["vv"], args.nx, S)
+        del d
         torch.cuda.empty_cache()
         pf = os.path.join(tmp, "paramfile.txt")
         with open(pf, "w") as f:
@@ -877,7 +907,7 @@ def bench_driver(args, rank, world, peak, peak_kind):
         "config": {"workload": f"wsg_run_paramfile: {nx}x{nx} grid, {P} w-planes, support {S}, "
                                f"{n} measurements (+1000 dropped) from {bytes_in} bytes of files",
                    "files": "page cache after the first read", "parallelism": f"replicas{world}"},
-        "precisions": res, "clocks": clk,
+        "precisions": res, "clocks": clk, "sectoring": sectoring,
         "cpu_baseline": {"value": cpu_read_s, "unit": "s to read the dataset", "cores": 1,
                          "kind": "port", "sample": "the whole dataset through the NumPy reader "
                                                    "restatement (oracle/binms_oracle.py)"},

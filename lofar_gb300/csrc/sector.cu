@@ -293,10 +293,13 @@ SecGeom make_geom(long n, long nsectors, int yaxis, double dx, double wsh)
     g.yaxis = yaxis;
     g.dx = dx;
     g.wsh = wsh;
-    const long long per_round = 32ll * (nsectors + 1);
-    g.R = (int)std::max<long long>(1, ((long long)n * (nsectors + 1) + 32ll * kMaxCounts - 1) /
-                                          (32ll * kMaxCounts));
-    (void)per_round;
+    // rounds per warp chunk: enough that count[][] stays within kMaxCounts,
+    // and about 64 K chunks otherwise (fewer counts to write and scan, still
+    // several chunks per resident warp)
+    const long long r_counts = ((long long)n * (nsectors + 1) + 32ll * kMaxCounts - 1) /
+                               (32ll * kMaxCounts);
+    const long long r_par = std::min<long long>(64, (long long)n / (32ll * 65536));
+    g.R = (int)std::max<long long>(1, std::max(r_counts, r_par));
     g.T = (n + 32ll * g.R - 1) / (32ll * g.R);
     return g;
 }
