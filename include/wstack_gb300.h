@@ -205,6 +205,24 @@ WSG_API int wsg_image_forward_host(wsg_plan *plan, long num_points, long freq_pe
                            const float *weight, void *image);
 WSG_API int wsg_image_adjoint_host(wsg_plan *plan, const void *image, void *out);
 
+/* Asynchronous forms of the two calls above, for a stream of imaging steps:
+ * they return at once, and wsg_plan_synchronize waits for everything
+ * submitted.  The inputs of a forward call are uploaded on a copy stream into
+ * one of two device slots while the previous call computes; outputs are
+ * downloaded on a second copy stream while the next call computes.  Host
+ * buffers must stay valid and unchanged (outputs: unread) until
+ * wsg_plan_synchronize returns; pinned host memory lets the copies overlap.
+ * The image's download (forward) and upload (adjoint) run on the compute
+ * stream (by a copy kernel when the host image is pinned and 16-byte
+ * aligned), so an adjoint call may take the host image its forward call
+ * writes. */
+WSG_API int wsg_image_forward_host_async(wsg_plan *plan, long num_points, long freq_per_chan,
+                                         long polarizations, const double *uu, const double *vv,
+                                         const double *ww, const float *vis_real,
+                                         const float *vis_img, const float *weight, void *image);
+WSG_API int wsg_image_adjoint_host_async(wsg_plan *plan, const void *image, void *out);
+WSG_API int wsg_plan_synchronize(wsg_plan *plan);
+
 /* Resident grid of the plan ([P][Ny][Nx] complex), for inspection. */
 WSG_API void *wsg_plan_grid(wsg_plan *plan);
 

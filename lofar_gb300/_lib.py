@@ -133,6 +133,9 @@ SIGNATURES = {
     "wsg_image_adjoint": (_I, [_P, _P, _P]),
     "wsg_image_forward_host": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
     "wsg_image_adjoint_host": (_I, [_P, _P, _P]),
+    "wsg_image_forward_host_async": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P]),
+    "wsg_image_adjoint_host_async": (_I, [_P, _P, _P]),
+    "wsg_plan_synchronize": (_I, [_P]),
     "wsg_plan_autotune": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P, _P, _I,
                                ctypes.POINTER(Tuning), ctypes.POINTER(Tuning), _I,
                                ctypes.POINTER(_I)]),

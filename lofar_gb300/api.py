@@ -268,6 +268,28 @@ class Plan:
         check(self.lib.wsg_image_adjoint_host(self._h, _ptr(image), _ptr(out)))
         return out
 
+    def image_forward_host_async(self, uu, vv, ww, vis_real, vis_img, weight, image_out,
+                                 freq_per_chan=1, polarizations=1):
+        """Asynchronous image_forward_host: returns at once; the host buffers
+        must stay untouched until synchronize()."""
+        n = int(uu.shape[0])
+        self._sync_stream()
+        check(self.lib.wsg_image_forward_host_async(
+            self._h, n, int(freq_per_chan), int(polarizations), _ptr(uu), _ptr(vv), _ptr(ww),
+            _ptr(vis_real), _ptr(vis_img), _ptr(weight), _ptr(image_out)))
+        self.n_binned = n
+        return image_out
+
+    def image_adjoint_host_async(self, image, out):
+        """Asynchronous image_adjoint_host (see image_forward_host_async)."""
+        self._sync_stream()
+        check(self.lib.wsg_image_adjoint_host_async(self._h, _ptr(image), _ptr(out)))
+        return out
+
+    def synchronize(self):
+        """Wait for every call submitted to the plan."""
+        check(self.lib.wsg_plan_synchronize(self._h))
+
     # -- tuning ---------------------------------------------------------------
     def autotune(self, uu, vv, ww, vis_real, vis_img, weight, iters: int = 3, freq_per_chan=1,
                  polarizations=1, image=None):

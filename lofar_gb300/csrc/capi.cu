@@ -8,6 +8,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cstdint>
 #include <mutex>
 #include <new>
 
@@ -301,6 +303,22 @@ int wsg_plan_create(wsg_plan **out, int grid_size_x, int grid_size_y, int num_w_
 int wsg_plan_destroy(wsg_plan *p)
 {
     if (!p) return WSG_OK;
+    if (p->a_ready) {
+        cudaStreamSynchronize(p->s_in);
+        cudaStreamSynchronize(p->s_out);
+        if (p->stream) cudaStreamSynchronize(p->stream);
+        cudaEvent_t ev[] = {p->e_in[0], p->e_in[1], p->e_free[0], p->e_free[1], p->e_adj,
+                            p->e_vis_down};
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+        cudaStreamDestroy(p->s_in);
+        cudaStreamDestroy(p->s_out);
+        for (auto &slot : p->a_in)
+            for (DevBuf &b : slot) b.release();
+        p->a_img_fwd.release();
+        p->a_img_adj.release();
+        p->a_vis.release();
+    }
     if (p->fft) cufftDestroy(p->fft);
     DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rec16, &p->partials, &p->rcell, &p->rfrac, &p->rval, &p->ridx,
                       &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi, &p->h_wt, &p->h_image,
@@ -634,6 +652,148 @@ int wsg_image_adjoint_host(wsg_plan *p, const void *image, void *out)
     WSG_TRY(wsg_image_adjoint(p, p->h_image.p, p->h_out.p));
     if (obytes)
         WSG_CUDA(cudaMemcpyAsync(out, p->h_out.p, obytes, cudaMemcpyDeviceToHost, p->stream));
+    WSG_CUDA(cudaStreamSynchronize(p->stream));
+    return WSG_OK;
+}
+
+// ---- asynchronous host pipeline ---------------------------------------------
+
+namespace {
+
+// A large copy is issued as 32 MiB pieces: copies of one direction from
+// different streams share the copy engines in order, and a latency-critical
+// small copy (the adjoint's image) must not queue behind a whole prefetch.
+cudaError_t copy_pieces(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind,
+                        cudaStream_t s)
+{
+    const size_t piece = (size_t)32 << 20;
+    for (size_t o = 0; o < bytes; o += piece) {
+        const cudaError_t e = cudaMemcpyAsync(static_cast<char *>(dst) + o,
+                                              static_cast<const char *>(src) + o,
+                                              bytes - o < piece ? bytes - o : piece, kind, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Copies between pinned host memory and the device done by a kernel on the
+// compute stream: they bypass the copy engines, where an image copy would
+// queue behind the next step's input upload (copies of one direction run in
+// order), and they sit on the compute stream's critical path, which is where
+// the image's round trip belongs.
+__global__ void k_copy16(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        dst[i] = src[i];
+}
+
+// dst <- src (bytes); `host` is whichever of the two is host memory.  Falls
+// back to cudaMemcpyAsync unless the host side is pinned and everything is
+// 16-byte aligned.
+cudaError_t copy_by_kernel(void *dst, const void *src, size_t bytes, const void *host,
+                           cudaMemcpyKind kind, cudaStream_t s)
+{
+    if (bytes == 0) return cudaSuccess;
+    cudaPointerAttributes a;
+    const bool pinned = cudaPointerGetAttributes(&a, host) == cudaSuccess &&
+                        a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
+    if (!pinned) cudaGetLastError();
+    const bool aligned = (((uintptr_t)dst | (uintptr_t)src | bytes) & 15) == 0;
+    if (!pinned || !aligned) return cudaMemcpyAsync(dst, src, bytes, kind, s);
+    // a.devicePointer is the device view of `host` itself
+    const void *dsrc = host == src ? a.devicePointer : src;
+    void *ddst = host == dst ? a.devicePointer : dst;
+    const size_t n = bytes / 16;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms() * 4);
+    k_copy16<<<blocks, 256, 0, s>>>(static_cast<const uint4 *>(dsrc), static_cast<uint4 *>(ddst), n);
+    return cudaGetLastError();
+}
+
+int ensure_async(wsg_plan *p)
+{
+    if (p->a_ready) return WSG_OK;
+    WSG_CUDA(cudaStreamCreateWithFlags(&p->s_in, cudaStreamNonBlocking));
+    WSG_CUDA(cudaStreamCreateWithFlags(&p->s_out, cudaStreamNonBlocking));
+    cudaEvent_t *ev[] = {&p->e_in[0], &p->e_in[1], &p->e_free[0], &p->e_free[1], &p->e_adj,
+                         &p->e_vis_down};
+    for (cudaEvent_t *e : ev) WSG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    p->a_ready = true;
+    return WSG_OK;
+}
+
+}  // namespace
+
+int wsg_image_forward_host_async(wsg_plan *p, long n, long nf, long np, const double *uu,
+                                 const double *vv, const double *ww, const float *vr,
+                                 const float *vi, const float *wt, void *image)
+{
+    clear_error();
+    if (!p || !image) return set_error(WSG_ERR_ARG, "NULL argument");
+    if (n < 0 || nf <= 0 || np <= 0) return set_error(WSG_ERR_ARG, "bad measurement counts");
+    if (n > 0 && (!uu || !vv || !ww || !vr || !vi || !wt))
+        return set_error(WSG_ERR_ARG, "NULL input pointer");
+    WSG_TRY(ensure_async(p));
+    const int s = p->a_slot;
+    const size_t nb = sizeof(double) * (size_t)n;
+    const size_t nvis = sizeof(float) * (size_t)n * nf * np;
+    const size_t nwt = sizeof(float) * (size_t)n * np;
+    const size_t bytes[6] = {nb, nb, nb, nvis, nvis, nwt};
+    const void *src[6] = {uu, vv, ww, vr, vi, wt};
+    for (int k = 0; k < 6; ++k) WSG_CUDA(p->a_in[s][k].ensure(bytes[k]));
+    WSG_CUDA(p->a_img_fwd.ensure(p->elem() * (size_t)p->npix()));
+    // the slot's previous inputs must have been binned before they are replaced
+    WSG_CUDA(cudaStreamWaitEvent(p->s_in, p->e_free[s], 0));
+    if (n > 0)
+        for (int k = 0; k < 6; ++k)
+            WSG_CUDA(copy_pieces(p->a_in[s][k].p, src[k], bytes[k], cudaMemcpyHostToDevice,
+                                 p->s_in));
+    WSG_CUDA(cudaEventRecord(p->e_in[s], p->s_in));
+    WSG_CUDA(cudaStreamWaitEvent(p->stream, p->e_in[s], 0));
+    WSG_TRY(wsg_image_forward(p, n, nf, np, p->a_in[s][0].as<double>(), p->a_in[s][1].as<double>(),
+                              p->a_in[s][2].as<double>(), p->a_in[s][3].as<float>(),
+                              p->a_in[s][4].as<float>(), p->a_in[s][5].as<float>(),
+                              p->a_img_fwd.p));
+    WSG_CUDA(cudaEventRecord(p->e_free[s], p->stream));
+    // the image download stays on the compute stream (see copy_by_kernel)
+    WSG_CUDA(copy_by_kernel(image, p->a_img_fwd.p, p->elem() * (size_t)p->npix(), image,
+                            cudaMemcpyDeviceToHost, p->stream));
+    p->a_slot = s ^ 1;
+    return WSG_OK;
+}
+
+int wsg_image_adjoint_host_async(wsg_plan *p, const void *image, void *out)
+{
+    clear_error();
+    if (!p || !image) return set_error(WSG_ERR_ARG, "NULL argument");
+    if (p->n_binned < 0) return set_error(WSG_ERR_STATE, "adjoint before a forward/bin call");
+    WSG_TRY(ensure_async(p));
+    const size_t ibytes = p->elem() * (size_t)p->npix();
+    const size_t obytes = p->elem() * (size_t)p->n_binned;
+    if (obytes && !out) return set_error(WSG_ERR_ARG, "NULL output");
+    WSG_CUDA(p->a_img_adj.ensure(ibytes));
+    WSG_CUDA(p->a_vis.ensure(obytes));
+    // on the compute stream, after the forward's download of the same host image
+    WSG_CUDA(copy_by_kernel(p->a_img_adj.p, image, ibytes, image, cudaMemcpyHostToDevice,
+                            p->stream));
+    // the previous adjoint output must have left the device buffer
+    WSG_CUDA(cudaStreamWaitEvent(p->stream, p->e_vis_down, 0));
+    WSG_TRY(wsg_image_adjoint(p, p->a_img_adj.p, p->a_vis.p));
+    WSG_CUDA(cudaEventRecord(p->e_adj, p->stream));
+    WSG_CUDA(cudaStreamWaitEvent(p->s_out, p->e_adj, 0));
+    if (obytes) WSG_CUDA(copy_pieces(out, p->a_vis.p, obytes, cudaMemcpyDeviceToHost, p->s_out));
+    WSG_CUDA(cudaEventRecord(p->e_vis_down, p->s_out));
+    return WSG_OK;
+}
+
+int wsg_plan_synchronize(wsg_plan *p)
+{
+    clear_error();
+    if (!p) return set_error(WSG_ERR_ARG, "plan is NULL");
+    if (p->a_ready) {
+        WSG_CUDA(cudaStreamSynchronize(p->s_in));
+        WSG_CUDA(cudaStreamSynchronize(p->s_out));
+    }
     WSG_CUDA(cudaStreamSynchronize(p->stream));
     return WSG_OK;
 }

@@ -105,6 +105,18 @@ struct wsg_plan {
     int fft_batch = 0;
     wsg::DevBuf fft_work;
 
+    // asynchronous host pipeline (wsg_image_*_host_async): input uploads on
+    // s_in into two slots, the adjoint output's download on s_out, compute
+    // and the image's round trip on `stream`
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t e_in[2] = {nullptr, nullptr};     // slot's inputs on the device
+    cudaEvent_t e_free[2] = {nullptr, nullptr};   // slot's inputs consumed
+    cudaEvent_t e_adj = nullptr;                  // adjoint output ready
+    cudaEvent_t e_vis_down = nullptr;             // adjoint output downloaded
+    wsg::DevBuf a_in[2][6], a_img_fwd, a_img_adj, a_vis;
+    int a_slot = 0;
+    bool a_ready = false;
+
     // FP32C fused FFT + w-correction (power-of-two grids)
     bool fused = false;
     bool tw_ready = false;
