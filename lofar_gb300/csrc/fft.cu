@@ -27,7 +27,11 @@
 // 256..8192.  Shared-memory index i is stored at i + i/16 so that the
 // butterfly strides hit distinct banks.  Twiddles come from a per-plan table
 // of e^{2 pi i m/N} computed in FP64 and rounded once to float.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "wsg_internal.cuh"
 
@@ -390,6 +394,52 @@ struct ColArgs {
     FftMasks m;
 };
 
+// ---- TMA staging of a column strip ---------------------------------------
+
+// Set when a CTA gave up waiting for its strip (the wait is bounded); read
+// by fft_tma_timed_out().
+__device__ int g_cols_tma_timeout;
+
+constexpr long kTmaWaitLimit = 1l << 22;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// box {2 complex, rows, 1 plane} at (x, y, z) into shared memory
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // Threads of a column-strip CTA: one per radix-16 butterfly of a column.
 template <int N> __host__ __device__ constexpr int col_threads() { return N / 16 < 512 ? N / 16 : 512; }
 
@@ -405,15 +455,20 @@ constexpr int kColsPerCta = 2;
 
 // Column FFTs of a strip of kColsPerCta adjacent columns of one plane (grid: x =
 // strip, y = plane).  Thread t owns butterfly t of every radix-16 pass of both
-// columns (same twiddles).  The first pass reads its 16 inputs straight from
-// HBM (rows t + r*N/16) and the last pass writes its 16 (or R) outputs straight
-// back, so shared memory only carries the passes in between: 4 shared-memory
-// accesses per point instead of 8 with staged loads and stores.  Forward:
-// rows of tiles without measurements are zero and not read.  Adjoint: only
-// rows of tiles the degridder reads are written.
+// columns (same twiddles).  The last pass writes its 16 (or R) outputs straight
+// back to HBM.  The first pass takes its 16 inputs (rows t + r*N/16):
+//   forward   straight from HBM, rows of tiles without measurements being zero
+//             and not read;
+//   adjoint, plain   from the strip staged in shared memory by the tensor
+//             memory accelerator: one thread issues one tile-high box per
+//             tile row, the CTA waits on an mbarrier (bounded), and the 16-byte
+//             row gathers of the direct loads leave the load/store pipeline.
+//             (Staging the sparse forward strips this way measured slower.)
+// Adjoint: only rows of tiles the degridder reads are written.
 template <int N, int S, int MODE>
-__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (kColsPerCta == 2 ? 2 : 3) : 1) k_cols(ColArgs a)
+__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (kColsPerCta == 2 ? 2 : 3) : 1) k_cols(ColArgs a, const __grid_constant__ CUtensorMap tmap)
 {
+    constexpr bool kStaged = MODE != kColsFwd;
     constexpr int NC = kColsPerCta;
     constexpr int T = col_threads<N>();
     constexpr int L16 = FftPlan<N>::L16;
@@ -422,7 +477,8 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (k
     static_assert(NB == T, "one radix-16 butterfly per thread");
     static_assert(L16 >= 2, "at least two radix-16 passes");
     constexpr int SC = col_stride<N>();
-    extern __shared__ __align__(16) float2 cbuf[];
+    extern __shared__ __align__(128) float2 cbuf[];
+    __shared__ __align__(8) unsigned long long s_bar;
     float2 *ca = cbuf, *cb = cbuf + SC;
     const int w = blockIdx.y;
     const int x0 = blockIdx.x * NC;
@@ -432,32 +488,57 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (k
     // this strip's tile-row mask (forward: tiles read; adjoint: tiles written)
     __shared__ unsigned char s_rows[N / 16];
     const int t = threadIdx.x;
+    static_assert(!kStaged || NC == 2, "a staged strip is two columns wide");
     if (MODE != kColsPlain)
         for (int tv = t; tv < a.ntv; tv += T)
             s_rows[tv] = MODE == kColsFwd ? a.m.occ_tile[((size_t)w * a.ntv + tv) * a.ntu + tu]
                                           : a.m.need_tile[((size_t)w * a.ntv + tv) * a.ntu + tu];
+    if (kStaged && t == 0) mbar_init(&s_bar);
     __syncthreads();
     float2 *col = a.grid + (size_t)w * a.ny * a.nx + x0;
     const size_t pitch = (size_t)a.nx;
+    float4 *stage = reinterpret_cast<float4 *>(cbuf);   // row r at stage[r]
 
-    // pass 0 (no twiddles): rows t + r*NB from HBM, outputs to 16t + r
+    if constexpr (kStaged) {
+        const int nbox = N >> a.tsh;
+        if (t == 0) {
+            mbar_expect_tx(&s_bar, (unsigned)(nbox * a.tile) * 16u);
+            for (int b = 0; b < nbox; b++)
+                tma_load_3d(stage + b * a.tile, &tmap, x0, b * a.tile, w, &s_bar);
+        }
+        bool done = false;
+        for (long it = 0; it < kTmaWaitLimit && !done; ++it) done = mbar_try_wait(&s_bar, 0);
+        if (!done) {
+            atomicExch(&g_cols_tma_timeout, 1);
+            // the copies may still be in flight: wait for them (bounded) before leaving
+            for (long it = 0; it < kTmaWaitLimit && !done; ++it) done = mbar_try_wait(&s_bar, 0);
+        }
+        if (__syncthreads_or(!done)) return;   // the whole CTA gives up together
+    }
+
+    // pass 0 (no twiddles): rows t + r*NB, outputs to 16t + r
     {
         float2 xa[16], xb[16];
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             const int row = t + r * NB;
-            if (NC == 2) {
+            if (kStaged) {
+                const float4 v = stage[row];
+                xa[r] = make_float2(v.x, v.y);
+                xb[r] = make_float2(v.z, v.w);
+            } else if (NC == 2) {
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (MODE != kColsFwd || s_rows[row >> a.tsh]) v = ld_row2(col + (size_t)row * pitch);
+                if (s_rows[row >> a.tsh]) v = ld_row2(col + (size_t)row * pitch);
                 xa[r] = make_float2(v.x, v.y);
                 xb[r] = make_float2(v.z, v.w);
             } else {
                 xa[r] = make_float2(0.f, 0.f);
-                if (MODE != kColsFwd || s_rows[row >> a.tsh]) xa[r] = __ldcg(col + (size_t)row * pitch);
+                if (s_rows[row >> a.tsh]) xa[r] = __ldcg(col + (size_t)row * pitch);
             }
         }
         dft16<S>(xa);
         if (NC == 2) dft16<S>(xb);
+        if (kStaged) __syncthreads();   // the strip is read: ca/cb overwrite it
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             ca[pidx(16 * t + r)] = xa[r];
@@ -786,6 +867,38 @@ template <int N> size_t row_smem(int planes, int ntu)
            (size_t)planes * ntu;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// The cube [planes][ny][nx] of 8-byte complex values as a 3D tensor; a box is
+// 2 values (16 bytes) wide, one tile high, one plane deep.
+cudaError_t cols_tensor_map(const ColArgs &a, int planes, CUtensorMap *m)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    if (a.nx % 2 || ((unsigned long long)(size_t)a.grid & 15) || a.tile > 256)
+        return cudaErrorInvalidValue;
+    const cuuint64_t dims[3] = {(cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)a.nx * 8, (cuuint64_t)a.nx * a.ny * 8};
+    const cuuint32_t box[3] = {2, (cuuint32_t)a.tile, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, a.grid, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 template <int N, int S, int MODE>
 cudaError_t run_cols(const ColArgs &a, int planes, cudaStream_t s)
 {
@@ -793,8 +906,14 @@ cudaError_t run_cols(const ColArgs &a, int planes, cudaStream_t s)
     cudaError_t e = cudaFuncSetAttribute(k_cols<N, S, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    CUtensorMap m;
+    memset(&m, 0, sizeof(m));   // unused by the forward
+    if (MODE != kColsFwd) {
+        e = cols_tensor_map(a, planes, &m);
+        if (e != cudaSuccess) return e;
+    }
     k_cols<N, S, MODE><<<dim3(a.nx / kColsPerCta, planes), col_threads<N>(),
-                         smem, s>>>(a);
+                         smem, s>>>(a, m);
     return cudaGetLastError();
 }
 
@@ -921,6 +1040,16 @@ cudaError_t launch_fft2d_plain(const GeomParams &g, float2 *grid, const float2 *
     if (e != cudaSuccess) return e;
     return sign > 0 ? rows_plain_dispatch<+1>(g.nx, grid, twx, g.ny, g.planes, s)
                     : rows_plain_dispatch<-1>(g.nx, grid, twx, g.ny, g.planes, s);
+}
+
+bool fft_tma_timed_out()
+{
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_cols_tma_timeout, sizeof(v)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return v != 0;
 }
 
 }  // namespace wsg

@@ -240,6 +240,9 @@ cudaError_t launch_image_adj_fused(const GeomParams &g, const float2 *image, flo
                                    const FftMasks &m, bool phase, double scale, cudaStream_t s);
 cudaError_t launch_fft2d_plain(const GeomParams &g, float2 *grid, const float2 *twx,
                                const float2 *twy, int sign, cudaStream_t s);
+// A column-FFT CTA gave up waiting for its TMA-staged strip (process-wide,
+// sticky): its columns were not transformed.
+bool fft_tma_timed_out();
 cudaError_t launch_f64_to_f32(const double2 *in, float2 *out, long long n, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float2 *in, double2 *out, long long n, cudaStream_t s);
 
