@@ -399,6 +399,8 @@ int wsg_plan_get_stats(wsg_plan *p, wsg_stats *s)
     WSG_CUDA(cudaStreamSynchronize(p->stream));
     if (fft_tma_timed_out())
         return set_error(WSG_ERR_CUDA, "a column FFT gave up waiting for its staged strip");
+    if (degrid_tma_timed_out())
+        return set_error(WSG_ERR_CUDA, "a degridding CTA gave up waiting for its staged tile");
     s->points_in = p->n_binned;
     s->records = (long long)c.records;
     s->dropped_plane = (long long)c.dropped_plane;

@@ -10,12 +10,17 @@
 // grid read as zero), then gathers the bin's primary records.  Duplicate
 // records of the bin are not visited: the halo makes every primary's window
 // local.
-//   FP32C: records staged kStage at a time; a group of 8 (or 16) lanes takes
+//   FP32C: the tile + halo arrives by TMA (below; plain loads on odd-width
+//   grids), records are staged kStage at a time; a group of 8 (or 16) lanes takes
 //   one record, lane k its row k: the row sum over the NT columns uses the
 //   column weights shuffled from the group's lanes, the row weight is applied
 //   once, and a shuffle tree over the group sums the rows.
 //   FP64: a warp takes one record, lanes take taps, a shuffle tree sums them.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "wsg_internal.cuh"
 
@@ -29,7 +34,41 @@ struct DegridArgs {
     RecBuffers r;
     const void *grid;
     void *out;
+    int tma;   // FP32C: the tile + halo is staged by TMA (even grid widths)
 };
+
+// ---- TMA staging of the tile + halo -------------------------------------
+//
+// FP32C on grids of even width: one thread loads the tile and its halo as one
+// 3D box (the tensor memory accelerator zero-fills the cells off the grid) and
+// the CTA waits on an mbarrier with a bounded try_wait loop; the per-cell
+// loads, bounds tests and shared-memory stores of the plain staging go away.
+
+// Set when a CTA gave up waiting for its tile (read by degrid_tma_timed_out).
+__device__ int g_degrid_tma_timeout;
+constexpr long kDegridWaitLimit = 1l << 22;
+
+__device__ __forceinline__ unsigned smem_u32d(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool mbar_try_wait_d(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32d(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Shared-memory pitch (complex values) of the TMA-staged tile: even (a TMA
+// box row is a multiple of 16 bytes) and 2 mod 4, so that the rows of one
+// record's window start in distinct 8-byte banks for up to 8 rows.
+template <int AW> __host__ __device__ constexpr int tma_pitch() { return (AW % 4 == 2) ? AW : AW + (AW % 2 ? 1 : 2 + (AW % 4 == 0 ? 0 : 2)); }
 
 __device__ __forceinline__ void decode_bin_d(const GeomParams &g, unsigned bin, int &w, int &u0,
                                              int &v0)
@@ -80,21 +119,25 @@ __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, 
 }
 
 template <int T, int K>
-__global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
+__global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __grid_constant__ CUtensorMap tmap)
 {
     constexpr int NT = 2 * K + 1;
     constexpr int GS = NT <= 8 ? 8 : 16;   // lanes per record (power of two)
     constexpr int RPW = 32 / GS;
     constexpr int H = 2 * K;
     constexpr int AW = T + 2 * H;
-    constexpr int AP = AW | 1;
+    constexpr int PW = tma_pitch<AW>();
+    constexpr int AP0 = AW | 1;
     constexpr int NW = kThreads / 32;
-    constexpr int TB = (AW * AP * 8 + 15) / 16 * 16;
-    extern __shared__ __align__(16) unsigned char smraw[];
+    constexpr int TB = ((AW * (PW > AP0 ? PW : AP0) * 8) + 127) / 128 * 128;
+    extern __shared__ __align__(128) unsigned char smraw[];
     float2 *tile = reinterpret_cast<float2 *>(smraw);
     uint4 *stage = reinterpret_cast<uint4 *>(smraw + TB);
     unsigned *sidx = reinterpret_cast<unsigned *>(smraw + TB + kStage * sizeof(uint4));
     __shared__ unsigned s_item;
+    __shared__ __align__(8) unsigned long long s_bar;
+    const int AP = a.tma ? PW : AP0;
+    unsigned phase = 0;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / GS, k = lane % GS;
@@ -107,6 +150,10 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
     float2 *out = reinterpret_cast<float2 *>(a.out);
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+    if (a.tma && tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32d(&s_bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
 
     for (;;) {
         __syncthreads();
@@ -120,13 +167,38 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a)
         decode_bin_d(a.g, bin, w, u0, v0);
         const unsigned off = a.b.off[bin];
         const size_t plane = (size_t)w * a.g.ny;
-        for (int i = tid; i < AW * AW; i += kThreads) {
-            const int y = i / AW, x = i - (i / AW) * AW;
-            const int gy = v0 - H + y, gx = u0 - H + x;
-            float2 val = make_float2(0.f, 0.f);
-            if (gx >= 0 && gx < a.g.nx && gy >= 0 && gy < a.g.ny)
-                val = grid[(plane + (size_t)gy) * a.g.nx + (size_t)gx];
-            tile[y * AP + x] = val;
+        if (a.tma) {
+            // one box: PW x AW values at (u0 - H, v0 - H) of plane w; cells
+            // off the grid read as zero
+            if (tid == 0) {
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                                 smem_u32d(&s_bar)),
+                             "r"((unsigned)(PW * AW * 8))
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                    "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32d(tile)),
+                    "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(u0 - H), "r"(v0 - H), "r"(w),
+                    "r"(smem_u32d(&s_bar))
+                    : "memory");
+            }
+            bool done = false;
+            for (long it = 0; it < kDegridWaitLimit && !done; ++it) done = mbar_try_wait_d(&s_bar, phase);
+            if (!done) {
+                atomicExch(&g_degrid_tma_timeout, 1);
+                for (long it = 0; it < kDegridWaitLimit && !done; ++it) done = mbar_try_wait_d(&s_bar, phase);
+            }
+            phase ^= 1u;
+            if (__syncthreads_or(!done)) return;   // the whole CTA gives up together
+        } else {
+            for (int i = tid; i < AW * AW; i += kThreads) {
+                const int y = i / AW, x = i - (i / AW) * AW;
+                const int gy = v0 - H + y, gx = u0 - H + x;
+                float2 val = make_float2(0.f, 0.f);
+                if (gx >= 0 && gx < a.g.nx && gy >= 0 && gy < a.g.ny)
+                    val = grid[(plane + (size_t)gy) * a.g.nx + (size_t)gx];
+                tile[y * AP + x] = val;
+            }
         }
         for (unsigned c0 = p0; c0 < p1; c0 += kStage) {
             const unsigned cnt = min((unsigned)kStage, p1 - c0);
@@ -269,7 +341,9 @@ template <int T, int K> size_t degrid_smem(int prec)
     if (prec == WSG_FP64) return (size_t)(T + 2 * K) * (T + 2 * K + 1) * sizeof(double2);
     constexpr int AW = T + 4 * K;
     constexpr int AP = AW | 1;
-    return ((size_t)AW * AP * 8 + 15) / 16 * 16 + (size_t)kStage * (sizeof(uint4) + sizeof(unsigned));
+    constexpr int PW = tma_pitch<AW>();
+    return ((size_t)AW * (PW > AP ? PW : AP) * 8 + 127) / 128 * 128 +
+           (size_t)kStage * (sizeof(uint4) + sizeof(unsigned));
 }
 
 template <int T, int K> const void *degrid_kernel(int prec)
@@ -300,6 +374,47 @@ const void *degrid_pick(int prec, int tile, int half, size_t &smem)
     return nullptr;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 degrid_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// The complex64 cube as a 3D tensor with a (tile + halo) box; false when the
+// grid cannot be described (odd width, unaligned base): the kernel then
+// stages with plain loads.
+bool degrid_tensor_map(const GeomParams &g, const void *grid, CUtensorMap *m)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = degrid_encoder();
+    if (!enc || (g.nx % 2) || ((size_t)grid & 15)) return false;
+    const int aw = g.tile + 4 * g.half;
+    int pw = aw;
+    switch (g.tile * 1000 + g.half) {   // tma_pitch<AW>() of the instantiated kernels
+#define WSG_PW(T, K) case T * 1000 + K: pw = tma_pitch<T + 4 * K>(); break;
+        WSG_PW(32, 0) WSG_PW(32, 1) WSG_PW(32, 2) WSG_PW(32, 3) WSG_PW(32, 4) WSG_PW(32, 5)
+        WSG_PW(32, 6) WSG_PW(32, 7) WSG_PW(64, 0) WSG_PW(64, 1) WSG_PW(64, 2) WSG_PW(64, 3)
+        WSG_PW(64, 4) WSG_PW(64, 5) WSG_PW(64, 6) WSG_PW(64, 7)
+#undef WSG_PW
+    default: return false;
+    }
+    if (pw > 256 || aw > 256) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 8, (cuuint64_t)g.nx * g.ny * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)pw, (cuuint32_t)aw, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(grid), dims, strides, box,
+               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 int degrid_max_ctas_per_sm(int prec, int tile, int half)
@@ -316,6 +431,16 @@ int degrid_max_ctas_per_sm(int prec, int tile, int half)
     return nb;
 }
 
+bool degrid_tma_timed_out()
+{
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_degrid_tma_timeout, sizeof(v)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return v != 0;
+}
+
 cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b, const RecBuffers &r,
                           const void *grid, void *out, long long n, int ctas, cudaStream_t s)
 {
@@ -327,8 +452,15 @@ cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b, co
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    DegridArgs a{g, b, r, grid, out};
-    void *args[] = {&a};
+    DegridArgs a{g, b, r, grid, out, 0};
+    if (prec == WSG_FP64) {
+        void *args[] = {&a};
+        return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
+    }
+    CUtensorMap m;
+    memset(&m, 0, sizeof(m));
+    a.tma = degrid_tensor_map(g, grid, &m) ? 1 : 0;
+    void *args[] = {&a, &m};
     return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
 }
 

@@ -243,6 +243,8 @@ cudaError_t launch_fft2d_plain(const GeomParams &g, float2 *grid, const float2 *
 // A column-FFT CTA gave up waiting for its TMA-staged strip (process-wide,
 // sticky): its columns were not transformed.
 bool fft_tma_timed_out();
+// The same for a degridding CTA and its TMA-staged tile.
+bool degrid_tma_timed_out();
 cudaError_t launch_f64_to_f32(const double2 *in, float2 *out, long long n, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float2 *in, double2 *out, long long n, cudaStream_t s);
 
