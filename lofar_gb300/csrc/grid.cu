@@ -9,7 +9,10 @@
 // (w-stacking.cu:35-118), whose FP64 global atomics scatter every tap to HBM.
 //
 // FP32C (k_grid_f32c): see the kernel's comment for the lane layout and the
-// fixed-point tile accumulator.  An item of a split bin writes its partial
+// fixed-point tile accumulator.  The accumulator's sums are exact integers and
+// each item's scale comes from an order-independent bound, so a bin that is
+// not split grids to the same bits whatever the order of its records.  An
+// item of a split bin writes its partial
 // tile (chunk 0 straight into the grid, the others into partial-tile slots);
 // the CTA that finishes a split bin's last item combines the bin's partials
 // cell by cell with TwoSum (hi + lo), in chunk order, so the error of a cell
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
     constexpr int NB = (AW + 7) / 8;   // 8x8-cell blocks of the accumulator
     __shared__ float s_part[NW];
     __shared__ float s_vmax[NW];
-    __shared__ float s_blk[NB * NB];
+    __shared__ unsigned s_blk[NB * NB];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / NT, k = lane - (lane / NT) * NT;
@@ -154,38 +157,54 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         // of the accumulator (by centre cell); a cell's taps all come from
         // records centred within K <= 7 cells, i.e. in its block or the 8
         // around it, so the largest 3x3-block sum times the peak weight norm
-        // bounds every cell of the item.
-        for (int i = tid; i < NB * NB; i += kThreads) s_blk[i] = 0.0f;
-        __syncthreads();
+        // bounds every cell of the item.  The block sums are integers: each
+        // term is rounded up at a scale taken from the item's largest value
+        // and record count (sums stay below 2^31), so the bound is an upper
+        // bound, independent of the order of the records, and costs integer
+        // shared-memory atomics instead of float ones.
+        for (int i = tid; i < NB * NB; i += kThreads) s_blk[i] = 0u;
         float vmax = 0.0f;
         for (unsigned i = r0 + tid; i < r1; i += kThreads) {
             const uint4 q = __ldcg(rec + off + i);
-            const int bx = ((int)(q.x >> 24) - 64 + H) >> 3;
-            const int by = ((int)(q.y >> 24) - 64 + H) >> 3;
-            const float ar = fabsf(__uint_as_float(q.z)), ai = fabsf(__uint_as_float(q.w));
-            vmax = fmaxf(vmax, fmaxf(ar, ai));
-            atomicAdd(&s_blk[by * NB + bx], ar + ai);
+            vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(q.z)), fabsf(__uint_as_float(q.w))));
         }
         for (int d = 16; d >= 1; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xFFFFFFFFu, vmax, d));
         if (lane == 0) s_vmax[warp] = vmax;
         __syncthreads();
-        float bmax = 0.0f;
-        for (int i = tid; i < NB * NB; i += kThreads) {
-            const int by = i / NB, bx = i - (i / NB) * NB;
-            float t = 0.0f;
-            for (int yy = max(by - 1, 0); yy <= min(by + 1, NB - 1); yy++)
-                for (int xx = max(bx - 1, 0); xx <= min(bx + 1, NB - 1); xx++)
-                    t += s_blk[yy * NB + xx];
-            bmax = fmaxf(bmax, t);
-        }
-        for (int d = 16; d >= 1; d >>= 1) bmax = fmaxf(bmax, __shfl_xor_sync(0xFFFFFFFFu, bmax, d));
-        if (lane == 0) s_part[warp] = bmax;
-        __syncthreads();
-        float bound = 0.0f, tapmax = 0.0f;
+        float tapmax = 0.0f;
 #pragma unroll
-        for (int i = 0; i < NW; i++) {
-            bound = fmaxf(bound, s_part[i]);
-            tapmax = fmaxf(tapmax, s_vmax[i]);
+        for (int i = 0; i < NW; i++) tapmax = fmaxf(tapmax, s_vmax[i]);
+        float bound = 0.0f;
+        if (tapmax > 0.0f) {
+            int ev;
+            frexpf(tapmax, &ev);                    // |Re V| + |Im V| < 2^(ev+1)
+            const int lb = 32 - __clz(r1 - r0);     // record count < 2^lb
+            const int sc = min(30 - lb - ev, 126);  // terms <= 2^(31-lb): sums < 2^31
+            const float up = ldexpf(1.0f, sc);
+            for (unsigned i = r0 + tid; i < r1; i += kThreads) {
+                const uint4 q = __ldcg(rec + off + i);
+                const int bx = ((int)(q.x >> 24) - 64 + H) >> 3;
+                const int by = ((int)(q.y >> 24) - 64 + H) >> 3;
+                const float v = fabsf(__uint_as_float(q.z)) + fabsf(__uint_as_float(q.w));
+                // v*up rounded up twice: the product toward +inf, then ceil
+                atomicAdd(&s_blk[by * NB + bx], (unsigned)ceilf(__fmul_ru(v, up)));
+            }
+            __syncthreads();
+            unsigned long long bmax = 0ull;
+            for (int i = tid; i < NB * NB; i += kThreads) {
+                const int by = i / NB, bx = i - (i / NB) * NB;
+                unsigned long long t = 0ull;
+                for (int yy = max(by - 1, 0); yy <= min(by + 1, NB - 1); yy++)
+                    for (int xx = max(bx - 1, 0); xx <= min(bx + 1, NB - 1); xx++)
+                        t += s_blk[yy * NB + xx];
+                bmax = max(bmax, t);
+            }
+            for (int d = 16; d >= 1; d >>= 1) bmax = max(bmax, __shfl_xor_sync(0xFFFFFFFFu, bmax, d));
+            if (lane == 0) s_part[warp] = __ull2float_ru(bmax);
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < NW; i++) bound = fmaxf(bound, s_part[i]);
+            bound = ldexpf(bound, -sc);
         }
         // cell sums stay below 2^30 (+ at most one rounding per term) and
         // every scaled tap below 2^22 (exact rounding with one FMA, below)
