@@ -243,7 +243,8 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
                                                   __float_as_uint((float)re),
                                                   __float_as_uint((float)im));
                     }
-                    r.idx[pos] = (unsigned)m;
+                    // only the degridder reads idx, and only of primaries
+                    if (tv == o.tvp && tu == o.tup) r.idx[pos] = (unsigned)m;
                 }
             }
         }
@@ -395,7 +396,7 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
                                                   __float_as_uint((float)re),
                                                   __float_as_uint((float)im));
                     }
-                    r.idx[pos] = idx;
+                    if (primary) r.idx[pos] = idx;   // read for primaries only
                 }
             }
         }
