@@ -34,7 +34,6 @@ struct DegridArgs {
     RecBuffers r;
     const void *grid;
     void *out;
-    int tma;   // FP32C: the tile + halo is staged by TMA (even grid widths)
 };
 
 // ---- TMA staging of the tile + halo -------------------------------------
@@ -67,7 +66,10 @@ __device__ __forceinline__ bool mbar_try_wait_d(unsigned long long *bar, unsigne
 
 // Shared-memory pitch (complex values) of the TMA-staged tile: even (a TMA
 // box row is a multiple of 16 bytes) and 2 mod 4, so that the rows of one
-// record's window start in distinct 8-byte banks for up to 8 rows.
+// record's window start in distinct 8-byte banks for up to 8 rows.  An even
+// pitch cannot separate more rows, so supports above 7 (9..15 rows) keep the
+// plain staging and its odd pitch: measured, TMA with the even pitch made
+// support 9 14 % slower.
 template <int AW> __host__ __device__ constexpr int tma_pitch() { return (AW % 4 == 2) ? AW : AW + (AW % 2 ? 1 : 2 + (AW % 4 == 0 ? 0 : 2)); }
 
 __device__ __forceinline__ void decode_bin_d(const GeomParams &g, unsigned bin, int &w, int &u0,
@@ -118,7 +120,7 @@ __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, 
     return p1 > p0;
 }
 
-template <int T, int K>
+template <int T, int K, bool TMA>
 __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __grid_constant__ CUtensorMap tmap)
 {
     constexpr int NT = 2 * K + 1;
@@ -129,14 +131,14 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     constexpr int PW = tma_pitch<AW>();
     constexpr int AP0 = AW | 1;
     constexpr int NW = kThreads / 32;
-    constexpr int TB = ((AW * (PW > AP0 ? PW : AP0) * 8) + 127) / 128 * 128;
-    extern __shared__ __align__(128) unsigned char smraw[];
+    constexpr int AP = TMA ? PW : AP0;
+    constexpr int TB = TMA ? (AW * PW * 8 + 127) / 128 * 128 : (AW * AP0 * 8 + 15) / 16 * 16;
+    extern __shared__ __align__(TMA ? 128 : 16) unsigned char smraw[];
     float2 *tile = reinterpret_cast<float2 *>(smraw);
     uint4 *stage = reinterpret_cast<uint4 *>(smraw + TB);
     unsigned *sidx = reinterpret_cast<unsigned *>(smraw + TB + kStage * sizeof(uint4));
     __shared__ unsigned s_item;
     __shared__ __align__(8) unsigned long long s_bar;
-    const int AP = a.tma ? PW : AP0;
     unsigned phase = 0;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     float2 *out = reinterpret_cast<float2 *>(a.out);
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
-    if (a.tma && tid == 0) {
+    if (TMA && tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32d(&s_bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -167,7 +169,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
         decode_bin_d(a.g, bin, w, u0, v0);
         const unsigned off = a.b.off[bin];
         const size_t plane = (size_t)w * a.g.ny;
-        if (a.tma) {
+        if constexpr (TMA) {
             // one box: PW x AW values at (u0 - H, v0 - H) of plane w; cells
             // off the grid read as zero
             if (tid == 0) {
@@ -336,30 +338,37 @@ __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
     }
 }
 
-template <int T, int K> size_t degrid_smem(int prec)
+// TMA staging serves supports up to 7 (window rows in distinct banks).
+constexpr int kDegridTmaMaxHalf = 3;
+
+template <int T, int K> size_t degrid_smem(int prec, bool tma)
 {
     if (prec == WSG_FP64) return (size_t)(T + 2 * K) * (T + 2 * K + 1) * sizeof(double2);
     constexpr int AW = T + 4 * K;
     constexpr int AP = AW | 1;
     constexpr int PW = tma_pitch<AW>();
-    return ((size_t)AW * (PW > AP ? PW : AP) * 8 + 127) / 128 * 128 +
-           (size_t)kStage * (sizeof(uint4) + sizeof(unsigned));
+    const size_t tile = tma ? ((size_t)AW * PW * 8 + 127) / 128 * 128
+                            : ((size_t)AW * AP * 8 + 15) / 16 * 16;
+    return tile + (size_t)kStage * (sizeof(uint4) + sizeof(unsigned));
 }
 
-template <int T, int K> const void *degrid_kernel(int prec)
+template <int T, int K> const void *degrid_kernel(int prec, bool tma)
 {
-    return prec == WSG_FP64 ? (const void *)k_degrid<T, K, double2>
-                            : (const void *)k_degrid_f32c<T, K>;
+    if (prec == WSG_FP64) return (const void *)k_degrid<T, K, double2>;
+    if constexpr (K <= kDegridTmaMaxHalf)
+        if (tma) return (const void *)k_degrid_f32c<T, K, true>;
+    return (const void *)k_degrid_f32c<T, K, false>;
 }
 
 template <int T>
-const void *degrid_select(int prec, int half, size_t &smem)
+const void *degrid_select(int prec, int half, bool tma, size_t &smem)
 {
+    tma = tma && prec != WSG_FP64 && half <= kDegridTmaMaxHalf;
     switch (half) {
 #define WSG_CASE(KK)                           \
     case KK:                                   \
-        smem = degrid_smem<T, KK>(prec);       \
-        return degrid_kernel<T, KK>(prec);
+        smem = degrid_smem<T, KK>(prec, tma);  \
+        return degrid_kernel<T, KK>(prec, tma);
         WSG_CASE(0) WSG_CASE(1) WSG_CASE(2) WSG_CASE(3)
         WSG_CASE(4) WSG_CASE(5) WSG_CASE(6) WSG_CASE(7)
 #undef WSG_CASE
@@ -367,10 +376,10 @@ const void *degrid_select(int prec, int half, size_t &smem)
     return nullptr;
 }
 
-const void *degrid_pick(int prec, int tile, int half, size_t &smem)
+const void *degrid_pick(int prec, int tile, int half, bool tma, size_t &smem)
 {
-    if (tile == 32) return degrid_select<32>(prec, half, smem);
-    if (tile == 64) return degrid_select<64>(prec, half, smem);
+    if (tile == 32) return degrid_select<32>(prec, half, tma, smem);
+    if (tile == 64) return degrid_select<64>(prec, half, tma, smem);
     return nullptr;
 }
 
@@ -420,7 +429,7 @@ bool degrid_tensor_map(const GeomParams &g, const void *grid, CUtensorMap *m)
 int degrid_max_ctas_per_sm(int prec, int tile, int half)
 {
     size_t smem = 0;
-    const void *k = degrid_pick(prec, tile, half, smem);
+    const void *k = degrid_pick(prec, tile, half, true, smem);
     if (!k) return 0;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
@@ -444,22 +453,23 @@ bool degrid_tma_timed_out()
 cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b, const RecBuffers &r,
                           const void *grid, void *out, long long n, int ctas, cudaStream_t s)
 {
+    CUtensorMap m;
+    memset(&m, 0, sizeof(m));
+    const bool tma = prec != WSG_FP64 && g.half <= kDegridTmaMaxHalf &&
+                     degrid_tensor_map(g, grid, &m);
     size_t smem = 0;
-    const void *k = degrid_pick(prec, g.tile, g.half, smem);
+    const void *k = degrid_pick(prec, g.tile, g.half, tma, smem);
     if (!k) return cudaErrorInvalidValue;
     const size_t esz = prec == WSG_FP64 ? sizeof(double2) : sizeof(float2);
     cudaError_t e = cudaMemsetAsync(out, 0, (size_t)n * esz, s);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    DegridArgs a{g, b, r, grid, out, 0};
+    DegridArgs a{g, b, r, grid, out};
     if (prec == WSG_FP64) {
         void *args[] = {&a};
         return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
     }
-    CUtensorMap m;
-    memset(&m, 0, sizeof(m));
-    a.tma = degrid_tensor_map(g, grid, &m) ? 1 : 0;
     void *args[] = {&a, &m};
     return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
 }
