@@ -212,10 +212,11 @@ WSG_API int wsg_image_adjoint_host(wsg_plan *plan, const void *image, void *out)
  * downloaded on a second copy stream while the next call computes.  Host
  * buffers must stay valid and unchanged (outputs: unread) until
  * wsg_plan_synchronize returns; pinned host memory lets the copies overlap.
- * The image's download (forward) and upload (adjoint) run on the compute
- * stream (by a copy kernel when the host image is pinned and 16-byte
- * aligned), so an adjoint call may take the host image its forward call
- * writes. */
+ * The image travels on the compute stream, so an adjoint call may take the
+ * host image its forward call writes: on FP32C power-of-two plans with a
+ * pinned host image the row kernels write and read the image rows in host
+ * memory directly; otherwise the image is copied (by a copy kernel when the
+ * host image is pinned and 16-byte aligned). */
 WSG_API int wsg_image_forward_host_async(wsg_plan *plan, long num_points, long freq_per_chan,
                                          long polarizations, const double *uu, const double *vv,
                                          const double *ww, const float *vis_real,

@@ -714,6 +714,19 @@ cudaError_t copy_by_kernel(void *dst, const void *src, size_t bytes, const void 
     return cudaGetLastError();
 }
 
+// The device's view of a pinned host buffer (8-byte aligned), or nullptr.
+void *pinned_view(const void *host)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer || ((uintptr_t)a.devicePointer & 7))
+        return nullptr;
+    return a.devicePointer;
+}
+
 int ensure_async(wsg_plan *p)
 {
     if (p->a_ready) return WSG_OK;
@@ -754,14 +767,19 @@ int wsg_image_forward_host_async(wsg_plan *p, long n, long nf, long np, const do
                                  p->s_in));
     WSG_CUDA(cudaEventRecord(p->e_in[s], p->s_in));
     WSG_CUDA(cudaStreamWaitEvent(p->stream, p->e_in[s], 0));
+    // A fused plan's row kernel writes each image row once: with a pinned host
+    // image it writes the rows straight into host memory, and the image's
+    // download leaves the critical path.
+    void *direct = p->fused ? pinned_view(image) : nullptr;
     WSG_TRY(wsg_image_forward(p, n, nf, np, p->a_in[s][0].as<double>(), p->a_in[s][1].as<double>(),
                               p->a_in[s][2].as<double>(), p->a_in[s][3].as<float>(),
                               p->a_in[s][4].as<float>(), p->a_in[s][5].as<float>(),
-                              p->a_img_fwd.p));
+                              direct ? direct : p->a_img_fwd.p));
     WSG_CUDA(cudaEventRecord(p->e_free[s], p->stream));
-    // the image download stays on the compute stream (see copy_by_kernel)
-    WSG_CUDA(copy_by_kernel(image, p->a_img_fwd.p, p->elem() * (size_t)p->npix(), image,
-                            cudaMemcpyDeviceToHost, p->stream));
+    // otherwise the download stays on the compute stream (see copy_by_kernel)
+    if (!direct)
+        WSG_CUDA(copy_by_kernel(image, p->a_img_fwd.p, p->elem() * (size_t)p->npix(), image,
+                                cudaMemcpyDeviceToHost, p->stream));
     p->a_slot = s ^ 1;
     return WSG_OK;
 }
@@ -775,14 +793,19 @@ int wsg_image_adjoint_host_async(wsg_plan *p, const void *image, void *out)
     const size_t ibytes = p->elem() * (size_t)p->npix();
     const size_t obytes = p->elem() * (size_t)p->n_binned;
     if (obytes && !out) return set_error(WSG_ERR_ARG, "NULL output");
-    WSG_CUDA(p->a_img_adj.ensure(ibytes));
     WSG_CUDA(p->a_vis.ensure(obytes));
-    // on the compute stream, after the forward's download of the same host image
-    WSG_CUDA(copy_by_kernel(p->a_img_adj.p, image, ibytes, image, cudaMemcpyHostToDevice,
-                            p->stream));
+    // A fused plan's adjoint row kernel reads each image row once: a pinned
+    // host image is read in place.  Otherwise it is uploaded on the compute
+    // stream, after the forward's download of the same host image.
+    const void *direct = p->fused ? pinned_view(image) : nullptr;
+    if (!direct) {
+        WSG_CUDA(p->a_img_adj.ensure(ibytes));
+        WSG_CUDA(copy_by_kernel(p->a_img_adj.p, image, ibytes, image, cudaMemcpyHostToDevice,
+                                p->stream));
+    }
     // the previous adjoint output must have left the device buffer
     WSG_CUDA(cudaStreamWaitEvent(p->stream, p->e_vis_down, 0));
-    WSG_TRY(wsg_image_adjoint(p, p->a_img_adj.p, p->a_vis.p));
+    WSG_TRY(wsg_image_adjoint(p, direct ? direct : p->a_img_adj.p, p->a_vis.p));
     WSG_CUDA(cudaEventRecord(p->e_adj, p->stream));
     WSG_CUDA(cudaStreamWaitEvent(p->s_out, p->e_adj, 0));
     if (obytes) WSG_CUDA(copy_pieces(out, p->a_vis.p, obytes, cudaMemcpyDeviceToHost, p->s_out));
