@@ -179,3 +179,23 @@ def test_device_cube_dump(gpu, tmp_path, precision, shape, scale):
     plan.close()
     os.remove(tmp_path / "re.bin")
     os.remove(tmp_path / "im.bin")
+
+
+def test_driver_grid_dump_matches_the_reference_own_dump(gpu, tmp_path, monkeypatch):
+    """The reference's own single-rank run (init.c reader, gridding.c sector
+    loop and WRITE_DATA dump, recorded in tests/golden/binms/ref_grid/) and
+    wsg_run_paramfile on the GPU read the same files with the same parameter
+    file; their grid dumps agree to FP64 summation order."""
+    from lofar_gb300 import binms
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "binms")
+    monkeypatch.chdir(gold)
+    p = binms.read_parameter_file("paramfile_grid.txt")
+    out = tmp_path / "out"
+    out.mkdir()
+    binms.run("paramfile_grid.txt", write_data=True, outdir=out, write_timings=False)
+    shape = (p["num_w_planes"], p["grid_size_y"], p["grid_size_x"])
+    got = binms.read_dump(out / f"0{p['outfile2']}", out / f"0{p['outfile3']}", shape)
+    ref = binms.read_dump(os.path.join(gold, "ref_grid", "0grid_real.bin"),
+                          os.path.join(gold, "ref_grid", "0grid_img.bin"), shape)
+    assert np.abs(ref).max() > 0
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
