@@ -464,9 +464,12 @@ constexpr int kColsPerCta = 2;
 //             tile row, the CTA waits on an mbarrier (bounded), and the 16-byte
 //             row gathers of the direct loads leave the load/store pipeline.
 //             (Staging the sparse forward strips this way measured slower.)
+//             The staged kernels run three CTAs per SM (at most 80 registers,
+//             a few spilled), the forward two: measured, three made the
+//             forward slower and the staged adjoint faster.
 // Adjoint: only rows of tiles the degridder reads are written.
 template <int N, int S, int MODE>
-__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (kColsPerCta == 2 ? 2 : 3) : 1) k_cols(ColArgs a, const __grid_constant__ CUtensorMap tmap)
+__global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (MODE == kColsFwd ? 2 : 3) : 1) k_cols(ColArgs a, const __grid_constant__ CUtensorMap tmap)
 {
     constexpr bool kStaged = MODE != kColsFwd;
     constexpr int NC = kColsPerCta;
