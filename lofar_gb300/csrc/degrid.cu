@@ -11,7 +11,7 @@
 // records of the bin are not visited: the halo makes every primary's window
 // local.
 //   FP32C: the tile + halo arrives by TMA (below; plain loads on odd-width
-//   grids), records are staged kStage at a time; a group of 8 (or 16) lanes takes
+//   grids), records are staged kStageD at a time; a group of 8 (or 16) lanes takes
 //   one record, lane k its row k: the row sum over the NT columns uses the
 //   column weights shuffled from the group's lanes, the row weight is applied
 //   once, and a shuffle tree over the group sums the rows.
@@ -27,6 +27,10 @@
 namespace wsg {
 
 namespace {
+
+// Records staged per pass: 384 (with the TMA-staged tile of support 7, four
+// CTAs fit an SM, against three with 512).
+constexpr int kStageD = 384;
 
 struct DegridArgs {
     GeomParams g;
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     extern __shared__ __align__(TMA ? 128 : 16) unsigned char smraw[];
     float2 *tile = reinterpret_cast<float2 *>(smraw);
     uint4 *stage = reinterpret_cast<uint4 *>(smraw + TB);
-    unsigned *sidx = reinterpret_cast<unsigned *>(smraw + TB + kStage * sizeof(uint4));
+    unsigned *sidx = reinterpret_cast<unsigned *>(smraw + TB + kStageD * sizeof(uint4));
     __shared__ unsigned s_item;
     __shared__ __align__(8) unsigned long long s_bar;
     unsigned phase = 0;
@@ -202,8 +206,8 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
                 tile[y * AP + x] = val;
             }
         }
-        for (unsigned c0 = p0; c0 < p1; c0 += kStage) {
-            const unsigned cnt = min((unsigned)kStage, p1 - c0);
+        for (unsigned c0 = p0; c0 < p1; c0 += kStageD) {
+            const unsigned cnt = min((unsigned)kStageD, p1 - c0);
             __syncthreads();
             for (unsigned i = tid; i < cnt; i += kThreads) {
                 stage[i] = __ldcs(a.r.rec16 + off + c0 + i);
@@ -349,7 +353,7 @@ template <int T, int K> size_t degrid_smem(int prec, bool tma)
     constexpr int PW = tma_pitch<AW>();
     const size_t tile = tma ? ((size_t)AW * PW * 8 + 127) / 128 * 128
                             : ((size_t)AW * AP * 8 + 15) / 16 * 16;
-    return tile + (size_t)kStage * (sizeof(uint4) + sizeof(unsigned));
+    return tile + (size_t)kStageD * (sizeof(uint4) + sizeof(unsigned));
 }
 
 template <int T, int K> const void *degrid_kernel(int prec, bool tma)
