@@ -615,6 +615,57 @@ def bench_batch(args, rank, world, peak, peak_kind):
     n_e2e = max(args.e2e_steps, 1)
     for _ in range(n_e2e):
         e2e_step()
+    blocking_s = (time.perf_counter() - t0) / n_e2e
+
+    # the same steps pipelined over three streams: a step's inputs are uploaded
+    # while the previous step's adjoint runs (the forward has binned the bound
+    # inputs by then), its images and model visibilities are downloaded while
+    # the next kernels run
+    comp = torch.cuda.current_stream()
+    copy_s, out_s = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def upload():
+        with torch.cuda.stream(copy_s):
+            for dst, src in zip(B._bound, host_in):
+                for d, h in zip(dst, src):
+                    d.copy_(h, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(copy_s)
+        return ev
+
+    def pipelined(k):
+        ev_in = upload()
+        ev_img = ev_vis = None
+        for i in range(k):
+            comp.wait_event(ev_in)
+            if ev_img is not None:
+                comp.wait_event(ev_img)   # the previous images have left the device buffer
+            B.forward(images, graph=True)
+            ev_fwd = torch.cuda.Event()
+            ev_fwd.record(comp)
+            if i + 1 < k:
+                copy_s.wait_event(ev_fwd)
+                ev_in = upload()
+            out_s.wait_event(ev_fwd)
+            with torch.cuda.stream(out_s):
+                himg.copy_(images, non_blocking=True)
+            ev_img = torch.cuda.Event()
+            ev_img.record(out_s)
+            if ev_vis is not None:
+                comp.wait_event(ev_vis)
+            B.adjoint(images, out)
+            ev_adj = torch.cuda.Event()
+            ev_adj.record(comp)
+            out_s.wait_event(ev_adj)
+            with torch.cuda.stream(out_s):
+                hout.copy_(out, non_blocking=True)
+            ev_vis = torch.cuda.Event()
+            ev_vis.record(out_s)
+        torch.cuda.synchronize()
+
+    pipelined(1)
+    t0 = time.perf_counter()
+    pipelined(n_e2e)
     e2e_s = (time.perf_counter() - t0) / n_e2e
     h2d = sum(int(h.numel() * h.element_size()) for ch in host_in for h in ch)
     d2h = int(himg.numel() * 8 + hout.numel() * 8)
@@ -673,7 +724,9 @@ def bench_batch(args, rank, world, peak, peak_kind):
         "gpu_launches": args.steps * 12,   # 9 forward kernels (graph) + 3 adjoint
         "clocks": clk, "binning": stats, "device_bytes": B.device_bytes(), "gen_s": gen_s,
         "e2e": {"value": nvis / e2e_s / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3, "steps": n_e2e,
+                "pipelined": "uploads overlap the previous adjoint, downloads the next kernels",
+                "blocking": {"value": nvis / blocking_s / 1e6, "ms_per_step": blocking_s * 1e3}},
         "cells": cells,
     }
 
