@@ -15,13 +15,15 @@
 //   one record, lane k its row k: the row sum over the NT columns uses the
 //   column weights shuffled from the group's lanes, the row weight is applied
 //   once, and a shuffle tree over the group sums the rows.
-//   FP64: a warp takes one record, lanes take taps, a shuffle tree sums them.
+//   FP64: the same group-per-record layout, with the FP64 weights of
+//   taps64.cuh (several records per warp-wide exponential pass).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
 
+#include "taps64.cuh"
 #include "wsg_internal.cuh"
 
 namespace wsg {
@@ -87,18 +89,6 @@ __device__ __forceinline__ void decode_bin_d(const GeomParams &g, unsigned bin, 
     v0 = tv * g.tile;
 }
 
-template <typename T2> struct Cx;
-template <> struct Cx<float2> {
-    using S = float;
-    static __device__ __forceinline__ float2 zero() { return make_float2(0.f, 0.f); }
-};
-template <> struct Cx<double2> {
-    using S = double;
-    static __device__ __forceinline__ double2 zero() { return make_double2(0.0, 0.0); }
-};
-
-__device__ __forceinline__ float gauss1d(float d) { return __expf(-0.5f * (d * d)); }
-__device__ __forceinline__ double gauss1d(double d) { return exp(-(d * d) * 0.5); }
 
 // Work item -> (bin, primaries [p0, p1)); the same items as the gridder.
 __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, unsigned nsplit,
@@ -247,38 +237,27 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     }
 }
 
-template <int T, int K, typename C2>
-__global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
+template <int T, int K>
+__global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
 {
-    using S = typename Cx<C2>::S;
-    constexpr int NT = 2 * K + 1;
-    constexpr int NTAP = NT * NT;
-    constexpr int ROUNDS = (NTAP + 31) / 32;
+    using P = Taps64<K>;
+    constexpr int NT = P::NT;
     constexpr int HW = T + 2 * K;      // tile + halo
     constexpr int SP = T + NT;         // smem pitch (== HW + 1)
     constexpr int NW = kThreads / 32;
     extern __shared__ unsigned char smraw[];
-    C2 *tile = reinterpret_cast<C2 *>(smraw);
+    double2 *tile = reinterpret_cast<double2 *>(smraw);
     __shared__ unsigned s_item;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const S norm = (S)(0.5 / kRefPi);
-    const C2 *__restrict__ grid = reinterpret_cast<const C2 *>(a.grid);
-    const C2 *__restrict__ fr_all = reinterpret_cast<const C2 *>(a.r.frac);
-    C2 *out = reinterpret_cast<C2 *>(a.out);
+    const int grp = lane / P::G, row = lane % P::G;
+    const double2 *__restrict__ grid = reinterpret_cast<const double2 *>(a.grid);
+    const double2 *__restrict__ fr_all = reinterpret_cast<const double2 *>(a.r.frac);
+    double2 *out = reinterpret_cast<double2 *>(a.out);
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
-
-    int odj[ROUNDS], odk[ROUNDS];
-#pragma unroll
-    for (int r = 0; r < ROUNDS; r++) {
-        const int l = lane + 32 * r;
-        odk[r] = (l < NTAP) ? l / NT : 4096;
-        odj[r] = l % NT;
-    }
-    const bool is_u = lane < NT;
-    const bool is_v = lane >= NT && lane < 2 * NT;
-    const S off1d = (S)((is_u ? lane : lane - NT) - K) + (S)0.5;
+    double nt_u, t_v;
+    taps64_consts<K>(lane, 0.5 / kRefPi, nt_u, t_v);
 
     for (;;) {
         __syncthreads();
@@ -295,48 +274,50 @@ __global__ void __launch_bounds__(kThreads) k_degrid(DegridArgs a)
         for (int i = tid; i < HW * HW; i += kThreads) {
             const int y = i / HW, x = i - (i / HW) * HW;
             const int gy = v0 - K + y, gx = u0 - K + x;
-            C2 val = Cx<C2>::zero();
+            double2 val = make_double2(0.0, 0.0);
             if (gx >= 0 && gx < a.g.nx && gy >= 0 && gy < a.g.ny)
                 val = grid[(plane + (size_t)gy) * a.g.nx + (size_t)gx];
             tile[y * SP + x] = val;
         }
         __syncthreads();
-        for (unsigned rr = p0 + warp; rr < p1; rr += NW) {
-            const unsigned cell = __ldg(a.r.cell + off + rr);
-            const C2 fr = fr_all[off + rr];
-            const unsigned idx = __ldg(a.r.idx + off + rr);
-            // window origin in halo-tile coordinates: (cell - K) - (-K) = cell
-            const int cu = (int)(cell & 0xFFFFu) - 32768;
-            const int cv = (int)(cell >> 16) - 32768;
-            // separable Gaussian: lanes [0,NT) hold norm*exp(-du^2/2) for
-            // column j, lanes [NT,2NT) exp(-dv^2/2) for row k
-            S e = 0;
-            if (is_u) e = norm * gauss1d(off1d - fr.x);
-            else if (is_v) e = gauss1d(off1d - fr.y);
-            S sr = 0, si = 0;
+        for (unsigned base = p0 + warp * P::RE; base < p1; base += NW * P::RE) {
+            const unsigned cnt = min((unsigned)P::RE, p1 - base);
+            double E[P::EP];
+            taps64_exps<K>(E, fr_all + off + base, cnt, lane);
 #pragma unroll
-            for (int r = 0; r < ROUNDS; r++) {
-                const S gu = __shfl_sync(0xFFFFFFFFu, e, odj[r]);
-                const S gv = __shfl_sync(0xFFFFFFFFu, e, (NT + odk[r]) & 31);
-                const int x = cu + odj[r];
-                const int y = cv + odk[r];
-                if ((unsigned)x < (unsigned)HW && (unsigned)y < (unsigned)HW) {
-                    const S wgt = gu * gv;
-                    const C2 g = tile[y * SP + x];
-                    sr += wgt * g.x;
-                    si += wgt * g.y;
+            for (int s = 0; s < P::SUB; s++) {
+                const int r = s * P::R + grp;
+                double gu, gv;
+                taps64_factors<K>(E, r, lane, nt_u, t_v, gu, gv);
+                unsigned cell = 0, idx = 0;
+                if ((unsigned)r < cnt) {
+                    cell = __ldg(a.r.cell + off + base + r);
+                    idx = __ldg(a.r.idx + off + base + r);
                 }
-            }
+                // window origin in halo-tile coordinates: (cell - K) - (-K) = cell;
+                // lane `row` sums row `row` of the window
+                const int cu = (int)(cell & 0xFFFFu) - 32768;
+                const int y = (int)(cell >> 16) - 32768 + row;
+                const bool on = (unsigned)r < cnt && row < NT && (unsigned)y < (unsigned)HW;
+                double sr = 0.0, si = 0.0;
 #pragma unroll
-            for (int d = 16; d >= 1; d >>= 1) {
-                sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
-                si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
-            }
-            if (lane == 0) {
-                C2 o;
-                o.x = sr;
-                o.y = si;
-                out[idx] = o;
+                for (int j = 0; j < NT; j++) {
+                    const double g = __shfl_sync(0xFFFFFFFFu, gu, grp * P::G + j);
+                    const int x = cu + j;
+                    if (on && (unsigned)x < (unsigned)HW) {
+                        const double2 t = tile[y * SP + x];
+                        sr = fma(g, t.x, sr);
+                        si = fma(g, t.y, si);
+                    }
+                }
+                sr *= gv;
+                si *= gv;
+#pragma unroll
+                for (int d = P::G / 2; d >= 1; d >>= 1) {
+                    sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
+                    si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
+                }
+                if (row == 0 && (unsigned)r < cnt) out[idx] = make_double2(sr, si);
             }
         }
     }
@@ -358,7 +339,7 @@ template <int T, int K> size_t degrid_smem(int prec, bool tma)
 
 template <int T, int K> const void *degrid_kernel(int prec, bool tma)
 {
-    if (prec == WSG_FP64) return (const void *)k_degrid<T, K, double2>;
+    if (prec == WSG_FP64) return (const void *)k_degrid_f64<T, K>;
     if constexpr (K <= kDegridTmaMaxHalf)
         if (tma) return (const void *)k_degrid_f32c<T, K, true>;
     return (const void *)k_degrid_f32c<T, K, false>;

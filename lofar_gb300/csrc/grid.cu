@@ -19,13 +19,14 @@
 // does not grow with the number of measurements that hit it.
 //
 // FP64 (k_grid_f64): whole bins (a split bin is processed by the CTA that
-// takes its first item); a warp takes one record and its lanes the
-// (2K+1)^2 taps; the tile's pitch T + 2K + 1 is congruent to the window
-// width modulo 16 doubles, so the taps of one window fall in distinct banks.
-// FP64 shared-memory atomics; the separable Gaussian
-// exp(-du^2/2)*exp(-dv^2/2) costs 2(2K+1) FP64 exponentials per record.
+// takes its first item), FP64 shared-memory atomics.  The kernel is bound by
+// FP64 instruction issue, so a warp takes several records at once
+// (taps64.cuh): six exponentials per record from one warp-wide pass, then a
+// group of G lanes per record, lane k scattering row k of the window; the
+// tile's pitch T + 2K + 1 puts the rows of one window in distinct banks.
 #include <cuda_runtime.h>
 
+#include "taps64.cuh"
 #include "wsg_internal.cuh"
 
 namespace wsg {
@@ -304,9 +305,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
 template <int T, int K>
 __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
 {
-    constexpr int NT = 2 * K + 1;
-    constexpr int NTAP = NT * NT;
-    constexpr int ROUNDS = (NTAP + 31) / 32;
+    using P = Taps64<K>;
+    constexpr int NT = P::NT;
     constexpr int PITCH = T + NT;
     constexpr int NW = kThreads / 32;
     extern __shared__ double smd[];
@@ -315,24 +315,14 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
     __shared__ unsigned s_item;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const double norm = 0.5 / kRefPi;
+    const int grp = lane / P::G, row = lane % P::G;
     const double2 *__restrict__ fr_all = reinterpret_cast<const double2 *>(a.r.frac);
     const double2 *__restrict__ val_all = reinterpret_cast<const double2 *>(a.r.val);
     double2 *grid = reinterpret_cast<double2 *>(a.grid);
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
-
-    int odj[ROUNDS], odk[ROUNDS];
-#pragma unroll
-    for (int r = 0; r < ROUNDS; r++) {
-        const int l = lane + 32 * r;
-        odk[r] = (l < NTAP) ? l / NT : 4096;
-        odj[r] = l % NT;
-    }
-    // lanes [0,NT) evaluate the u-factors, lanes [NT,2NT) the v-factors
-    const bool is_u = lane < NT;
-    const bool is_v = lane >= NT && lane < 2 * NT;
-    const double off1d = (double)((is_u ? lane : lane - NT) - K) + 0.5;
+    double nt_u, t_v;
+    taps64_consts<K>(lane, 0.5 / kRefPi, nt_u, t_v);
 
     for (int i = tid; i < 2 * T * PITCH; i += kThreads) smd[i] = 0.0;
 
@@ -351,32 +341,35 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         const unsigned off = a.b.off[bin];
         const unsigned n = a.b.ntotal[bin];
 
-        for (unsigned rr = warp; rr < n; rr += NW) {
-            const unsigned cell = __ldg(a.r.cell + off + rr);
-            const double2 fr = __ldg(fr_all + off + rr);
-            const double2 v = __ldg(val_all + off + rr);
-            const int cu = (int)(cell & 0xFFFFu) - 32768 - K;
-            const int cv = (int)(cell >> 16) - 32768 - K;
-            // j + 0.5 - pos == (j - cell) + 0.5 - frac, the same rounded value
-            // as the reference's u_dist (w-stacking.cu:85,89)
-            double e = 0.0;
-            if (is_u) {
-                const double d = off1d - fr.x;
-                e = norm * exp(-(d * d) * 0.5);
-            } else if (is_v) {
-                const double d = off1d - fr.y;
-                e = exp(-(d * d) * 0.5);
-            }
+        for (unsigned base = warp * P::RE; base < n; base += NW * P::RE) {
+            const unsigned cnt = min((unsigned)P::RE, n - base);
+            double E[P::EP];
+            taps64_exps<K>(E, fr_all + off + base, cnt, lane);
 #pragma unroll
-            for (int r = 0; r < ROUNDS; r++) {
-                const double gu = __shfl_sync(0xFFFFFFFFu, e, odj[r]);
-                const double gv = __shfl_sync(0xFFFFFFFFu, e, (NT + odk[r]) & 31);
-                const int x = cu + odj[r];
-                const int y = cv + odk[r];
-                if ((unsigned)x < (unsigned)tx && (unsigned)y < (unsigned)ty) {
-                    const double wgt = gu * gv;
-                    atomicAdd(sre + y * PITCH + x, wgt * v.x);
-                    atomicAdd(sim + y * PITCH + x, wgt * v.y);
+            for (int s = 0; s < P::SUB; s++) {
+                const int r = s * P::R + grp;
+                double gu, gv;
+                taps64_factors<K>(E, r, lane, nt_u, t_v, gu, gv);
+                unsigned cell = 0;
+                double2 v = make_double2(0.0, 0.0);
+                if ((unsigned)r < cnt) {
+                    cell = __ldg(a.r.cell + off + base + r);
+                    v = __ldg(val_all + off + base + r);
+                }
+                // window origin; lane `row` scatters row `row` of the window
+                const int cu = (int)(cell & 0xFFFFu) - 32768 - K;
+                const int y = (int)(cell >> 16) - 32768 - K + row;
+                const bool on = (unsigned)r < cnt && row < NT && (unsigned)y < (unsigned)ty;
+                const double au = gu * v.x, bu = gu * v.y;
+#pragma unroll
+                for (int j = 0; j < NT; j++) {
+                    const double tr = __shfl_sync(0xFFFFFFFFu, au, grp * P::G + j);
+                    const double ti = __shfl_sync(0xFFFFFFFFu, bu, grp * P::G + j);
+                    const int x = cu + j;
+                    if (on && (unsigned)x < (unsigned)tx) {
+                        atomicAdd(sre + y * PITCH + x, tr * gv);
+                        atomicAdd(sim + y * PITCH + x, ti * gv);
+                    }
                 }
             }
         }
