@@ -19,8 +19,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwstack_gb300.so")
 
-SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "capi.cu", "batch.cu",
-           "noalloc.cu", "binms.cu", "driver.cu", "sector.cu"]
+SOURCES = ["bin.cu", "grid.cu", "degrid.cu", "wcorrect.cu", "fft.cu", "fft64.cu", "capi.cu",
+           "batch.cu", "noalloc.cu", "binms.cu", "driver.cu", "sector.cu"]
 # the reference's executable (main.c) over the library: wstack_gb300_run PARAMFILE ...
 RUNNER_SRC = "wstack_run.cpp"
 RUNNER = os.path.join(HERE, "wstack_gb300_run")

@@ -136,6 +136,8 @@ int wsg::plan_configure(wsg_plan *p)
     const char *fft_env = getenv("WSTACK_GB300_FFT");
     p->fused = p->prec == WSG_FP32C && fft_fused_supported(p->nx, p->ny, p->tile) &&
                !(fft_env && strcmp(fft_env, "cufft") == 0);
+    p->fft64 = p->prec == WSG_FP64 && fft64_supported(p->nx, p->ny) &&
+               !(fft_env && strcmp(fft_env, "cufft") == 0);
     p->masks_valid = false;
     p->ctas_grid = p->ctas_user > 0 ? p->ctas_user : og * sms;
     p->ctas_degrid = p->ctas_user > 0 ? p->ctas_user : od * sms;
@@ -469,6 +471,19 @@ int wsg_fft(wsg_plan *p, void *grid, int sign)
         WSG_TRY(ensure_fused(p));
         WSG_CUDA(launch_fft2d_plain(p->geom, reinterpret_cast<float2 *>(grid), p->twx.as<float2>(),
                                     p->twy.as<float2>(), sign, p->stream));
+        return WSG_OK;
+    }
+    if (p->fft64) {
+        if (!p->tw64_ready) {
+            WSG_CUDA(p->tw64x.ensure((size_t)2 * p->nx * sizeof(int4)));
+            WSG_CUDA(p->tw64y.ensure((size_t)2 * p->ny * sizeof(int4)));
+            WSG_CUDA(build_twiddles64(p->tw64x.as<int4>(), p->nx, p->stream));
+            WSG_CUDA(build_twiddles64(p->tw64y.as<int4>(), p->ny, p->stream));
+            p->tw64_ready = true;
+        }
+        WSG_CUDA(launch_fft64(reinterpret_cast<double2 *>(grid), p->nx, p->ny,
+                              (int)p->cube_planes(), sign, p->tw64x.as<int4>(),
+                              p->tw64y.as<int4>(), 0, p->stream));
         return WSG_OK;
     }
     WSG_TRY(ensure_fft(p));
@@ -844,6 +859,8 @@ struct Legacy {
     cufftHandle fft = 0;
     int fft_nx = 0, fft_ny = 0, fft_batch = 0;
     DevBuf fft_work, fft_buf;
+    int tw64_nx = 0, tw64_ny = 0;   // twiddles of the integer-pipe FFT
+    DevBuf tw64x, tw64y;
 };
 
 Legacy &legacy()
@@ -990,7 +1007,17 @@ int legacy_fft(const double *in, double *out, int nx, int ny, int nplanes)
     WSG_TRY(legacy_stream(L));
     const long long npix = (long long)nx * ny;
     const size_t bytes = sizeof(double2) * (size_t)npix * nplanes;
-    if (!L.fft || L.fft_nx != nx || L.fft_ny != ny) {
+    const char *fft_env = getenv("WSTACK_GB300_FFT");
+    const bool int_fft = fft64_supported(nx, ny) && !(fft_env && strcmp(fft_env, "cufft") == 0);
+    if (int_fft && (L.tw64_nx != nx || L.tw64_ny != ny)) {
+        WSG_CUDA(L.tw64x.ensure((size_t)2 * nx * sizeof(int4)));
+        WSG_CUDA(L.tw64y.ensure((size_t)2 * ny * sizeof(int4)));
+        WSG_CUDA(build_twiddles64(L.tw64x.as<int4>(), nx, L.stream));
+        WSG_CUDA(build_twiddles64(L.tw64y.as<int4>(), ny, L.stream));
+        L.tw64_nx = nx;
+        L.tw64_ny = ny;
+    }
+    if (!int_fft && (!L.fft || L.fft_nx != nx || L.fft_ny != ny)) {
         if (L.fft) cufftDestroy(L.fft);
         L.fft = 0;
         WSG_CUFFT(cufftCreate(&L.fft));
@@ -1004,7 +1031,7 @@ int legacy_fft(const double *in, double *out, int nx, int ny, int nplanes)
         L.fft_nx = nx;
         L.fft_ny = ny;
     }
-    WSG_CUFFT(cufftSetStream(L.fft, L.stream));
+    if (!int_fft) WSG_CUFFT(cufftSetStream(L.fft, L.stream));
     const bool in_dev = device_accessible(in), out_dev = device_accessible(out);
     double2 *work;
     if (out_dev) {
@@ -1018,11 +1045,19 @@ int legacy_fft(const double *in, double *out, int nx, int ny, int nplanes)
         WSG_CUDA(cudaMemcpyAsync(work, in, bytes, in_dev ? cudaMemcpyDeviceToDevice
                                                          : cudaMemcpyHostToDevice, L.stream));
     }
-    for (int w = 0; w < nplanes; w++) {
-        cufftDoubleComplex *x = reinterpret_cast<cufftDoubleComplex *>(work) + (size_t)w * npix;
-        WSG_CUFFT(cufftExecZ2Z(L.fft, x, x, CUFFT_INVERSE));
+    if (int_fft) {
+        // 1/(nx ny) is an exact power of two, applied as the FFT's output exponent
+        int lg = 0;
+        while ((1ll << lg) < npix) lg++;
+        WSG_CUDA(launch_fft64(work, nx, ny, nplanes, +1, L.tw64x.as<int4>(), L.tw64y.as<int4>(),
+                              -lg, L.stream));
+    } else {
+        for (int w = 0; w < nplanes; w++) {
+            cufftDoubleComplex *x = reinterpret_cast<cufftDoubleComplex *>(work) + (size_t)w * npix;
+            WSG_CUFFT(cufftExecZ2Z(L.fft, x, x, CUFFT_INVERSE));
+        }
+        WSG_CUDA(launch_scale_f64(work, npix * nplanes, 1.0 / (double)npix, L.stream));
     }
-    WSG_CUDA(launch_scale_f64(work, npix * nplanes, 1.0 / (double)npix, L.stream));
     if (!out_dev) WSG_CUDA(cudaMemcpyAsync(out, work, bytes, cudaMemcpyDeviceToHost, L.stream));
     WSG_CUDA(cudaStreamSynchronize(L.stream));
     return WSG_OK;
@@ -1083,8 +1118,10 @@ void wstack_gb300_release(void)
     L.plan = nullptr;
     if (L.fft) cufftDestroy(L.fft);
     L.fft = 0;
+    L.tw64_nx = L.tw64_ny = 0;
     DevBuf *bufs[] = {&L.uu, &L.vv, &L.ww, &L.vr, &L.vi, &L.wt, &L.grid64, &L.image_re,
-                      &L.image_im, &L.planes, &L.sinx, &L.siny, &L.fft_work, &L.fft_buf};
+                      &L.image_im, &L.planes, &L.sinx, &L.siny, &L.fft_work, &L.fft_buf,
+                      &L.tw64x, &L.tw64y};
     for (DevBuf *b : bufs) b->release();
     if (L.stream) cudaStreamDestroy(L.stream);
     L.stream = nullptr;

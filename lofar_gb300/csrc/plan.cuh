@@ -117,6 +117,11 @@ struct wsg_plan {
     int a_slot = 0;
     bool a_ready = false;
 
+    // FP64 integer-pipe FFT (power-of-two grids)
+    bool fft64 = false;
+    bool tw64_ready = false;
+    wsg::DevBuf tw64x, tw64y;
+
     // FP32C fused FFT + w-correction (power-of-two grids)
     bool fused = false;
     bool tw_ready = false;
