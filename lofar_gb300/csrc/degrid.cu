@@ -282,8 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
         __syncthreads();
         for (unsigned base = p0 + warp * P::RE; base < p1; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, p1 - base);
-            double E[P::EP];
-            taps64_exps<K>(E, fr_all + off + base, cnt, lane);
+            const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
 #pragma unroll
             for (int s = 0; s < P::SUB; s++) {
                 const int r = s * P::R + grp;

@@ -343,8 +343,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
 
         for (unsigned base = warp * P::RE; base < n; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, n - base);
-            double E[P::EP];
-            taps64_exps<K>(E, fr_all + off + base, cnt, lane);
+            const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
 #pragma unroll
             for (int s = 0; s < P::SUB; s++) {
                 const int r = s * P::R + grp;
