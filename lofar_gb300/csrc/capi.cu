@@ -152,9 +152,8 @@ int wsg::ensure_records(wsg_plan *p, long long n)
     const unsigned long long need = (unsigned long long)(n > 0 ? n : 1) * 4ull;
     if (need <= p->rec_cap) return WSG_OK;
     WSG_CUDA(p->bins.ensure(bin_buffer_bytes(p->geom.nbins, max_split_items(need, p->split), kSub)));
-    if (p->prec == WSG_FP32C)
-        WSG_CUDA(p->partials.ensure(max_slots(need, p->split) * (size_t)p->tile * p->tile *
-                                    sizeof(float2)));
+    WSG_CUDA(p->partials.ensure(max_slots(need, p->split) * (size_t)p->tile * p->tile *
+                                (p->prec == WSG_FP64 ? sizeof(double2) : sizeof(float2))));
     WSG_CUDA(p->ridx.ensure(need * sizeof(unsigned)));
     if (p->prec == WSG_FP64) {
         WSG_CUDA(p->rcell.ensure(need * sizeof(unsigned)));

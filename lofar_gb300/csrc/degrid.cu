@@ -23,6 +23,7 @@
 
 #include <cstring>
 
+#include "fixed64.cuh"
 #include "taps64.cuh"
 #include "wsg_internal.cuh"
 
@@ -247,7 +248,8 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
     constexpr int NW = kThreads / 32;
     extern __shared__ unsigned char smraw[];
     double2 *tile = reinterpret_cast<double2 *>(smraw);
-    __shared__ unsigned s_item;
+    int4 *tfix = reinterpret_cast<int4 *>(smraw);   // the same cells in fixed point
+    __shared__ unsigned s_item, s_exp;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / P::G, row = lane % P::G;
@@ -261,7 +263,10 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_degrid, 1u);
+        if (tid == 0) {
+            s_item = atomicAdd(&a.b.ctr->work_degrid, 1u);
+            s_exp = 0u;
+        }
         __syncthreads();
         const unsigned item = s_item;
         if (item >= nitems) break;
@@ -271,6 +276,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
         decode_bin_d(a.g, bin, w, u0, v0);
         const unsigned off = a.b.off[bin];
         const size_t plane = (size_t)w * a.g.ny;
+        unsigned ex = 0u;
         for (int i = tid; i < HW * HW; i += kThreads) {
             const int y = i / HW, x = i - (i / HW) * HW;
             const int gy = v0 - K + y, gx = u0 - K + x;
@@ -278,8 +284,27 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
             if (gx >= 0 && gx < a.g.nx && gy >= 0 && gy < a.g.ny)
                 val = grid[(plane + (size_t)gy) * a.g.nx + (size_t)gx];
             tile[y * SP + x] = val;
+            ex = max(ex, max(exp_field(val.x), exp_field(val.y)));
         }
+        ex = __reduce_max_sync(0xFFFFFFFFu, ex);
+        if (lane == 0) atomicMax(&s_exp, ex);
         __syncthreads();
+        // The tile's scale: every |cell| < 2^(e - 1022), so cells times 2^s,
+        // s = 61 - (e - 1022), are below 2^61; a tile holding a NaN or an
+        // infinity (e = 2047) is gathered in FP64 instead.
+        const int e = (int)s_exp;
+        const bool fixed = e < 2047;
+        const int sc = min(61 - (e - 1022), 1020);
+        if (fixed) {
+            for (int i = tid; i < HW * HW; i += kThreads) {
+                const int y = i / HW, x = i - (i / HW) * HW;
+                const double2 val = tile[y * SP + x];
+                const Half64 hr = split64(to_fixed(__double_as_longlong(val.x), sc));
+                const Half64 hi = split64(to_fixed(__double_as_longlong(val.y), sc));
+                tfix[y * SP + x] = make_int4(hr.h, hr.l, hi.h, hi.l);
+            }
+            __syncthreads();
+        }
         for (unsigned base = p0 + warp * P::RE; base < p1; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, p1 - base);
             const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
@@ -298,25 +323,56 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
                 const int cu = (int)(cell & 0xFFFFu) - 32768;
                 const int y = (int)(cell >> 16) - 32768 + row;
                 const bool on = (unsigned)r < cnt && row < NT && (unsigned)y < (unsigned)HW;
-                double sr = 0.0, si = 0.0;
+                double2 o;
+                if (fixed) {
+                    // sum_j (cell 2^s)(gu 2^62) / 2^64, times (gv 2^62) / 2^64:
+                    // the result carries 2^(s-4); partial sums stay below 2^63
+                    const Half64 u = split64(to_fixed(__double_as_longlong(gu), 62));
+                    const Half64 g = split64(to_fixed(__double_as_longlong(gv), 62));
+                    long long sr = 0, si = 0;
 #pragma unroll
-                for (int j = 0; j < NT; j++) {
-                    const double g = __shfl_sync(0xFFFFFFFFu, gu, grp * P::G + j);
-                    const int x = cu + j;
-                    if (on && (unsigned)x < (unsigned)HW) {
-                        const double2 t = tile[y * SP + x];
-                        sr = fma(g, t.x, sr);
-                        si = fma(g, t.y, si);
+                    for (int j = 0; j < NT; j++) {
+                        const int src = grp * P::G + j;
+                        const Half64 uj = {__shfl_sync(0xFFFFFFFFu, u.h, src),
+                                           __shfl_sync(0xFFFFFFFFu, u.l, src)};
+                        const int x = cu + j;
+                        if (on && (unsigned)x < (unsigned)HW) {
+                            const int4 t = tfix[y * SP + x];
+                            sr += mulhi_bal({t.x, t.y}, uj);
+                            si += mulhi_bal({t.z, t.w}, uj);
+                        }
                     }
-                }
-                sr *= gv;
-                si *= gv;
+                    sr = mulhi_bal(split64(sr), g);
+                    si = mulhi_bal(split64(si), g);
 #pragma unroll
-                for (int d = P::G / 2; d >= 1; d >>= 1) {
-                    sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
-                    si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
+                    for (int d = P::G / 2; d >= 1; d >>= 1) {
+                        sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
+                        si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
+                    }
+                    o = make_double2(__longlong_as_double(from_fixed(sr, 4 - sc)),
+                                     __longlong_as_double(from_fixed(si, 4 - sc)));
+                } else {
+                    double sr = 0.0, si = 0.0;
+#pragma unroll
+                    for (int j = 0; j < NT; j++) {
+                        const double gj = __shfl_sync(0xFFFFFFFFu, gu, grp * P::G + j);
+                        const int x = cu + j;
+                        if (on && (unsigned)x < (unsigned)HW) {
+                            const double2 t = tile[y * SP + x];
+                            sr = fma(gj, t.x, sr);
+                            si = fma(gj, t.y, si);
+                        }
+                    }
+                    sr *= gv;
+                    si *= gv;
+#pragma unroll
+                    for (int d = P::G / 2; d >= 1; d >>= 1) {
+                        sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
+                        si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
+                    }
+                    o = make_double2(sr, si);
                 }
-                if (row == 0 && (unsigned)r < cnt) out[idx] = make_double2(sr, si);
+                if (row == 0 && (unsigned)r < cnt) out[idx] = o;
             }
         }
     }

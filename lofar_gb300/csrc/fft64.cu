@@ -24,6 +24,7 @@
 // The FFT is unnormalised, like FFTW's: sign +1 is exponent +i.
 #include <cuda_runtime.h>
 
+#include "fixed64.cuh"
 #include "wsg_internal.cuh"
 
 namespace wsg {
@@ -181,42 +182,6 @@ __device__ __forceinline__ int fft64_shift(unsigned hi)
 {
     const int e = (int)(hi >> 20);          // biased exponent: max < 2^(e - 1022)
     return min(61 - (e - 1022), 1000);
-}
-
-// Conversions between FP64 and the scaled integers with integer instructions
-// only (the FP64 conversion and multiply would issue at the FP64 rate).
-// round(x * 2^s) for |x| * 2^s < 2^62; ties round away from zero.
-__device__ __forceinline__ long long to_fixed(long long bits, int s)
-{
-    const int e = (int)((bits >> 52) & 0x7FF);
-    const long long m = (bits & 0xFFFFFFFFFFFFFll) | (e ? 0x10000000000000ll : 0ll);
-    const int sh = max(e, 1) - 1075 + s;      // |x| 2^s = m 2^sh
-    long long r;
-    if (sh >= 0)
-        r = m << sh;
-    else if (sh > -64)
-        r = (m + (1ll << (-sh - 1))) >> (-sh);
-    else
-        r = 0;
-    return bits < 0 ? -r : r;
-}
-
-// v * 2^k as an FP64 bit pattern, rounded to nearest even; the result is
-// assumed to be a normal number (|v| >= 1, k within the exponent range).
-__device__ __forceinline__ long long from_fixed(long long v, int k)
-{
-    if (v == 0) return 0;
-    const unsigned long long neg = v < 0 ? 0x8000000000000000ull : 0ull;
-    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-    const int lz = __clzll((long long)a);
-    const unsigned long long n = a << lz;                  // top bit set
-    unsigned long long mant = n >> 11;                     // 53 bits, hidden bit included
-    const unsigned long long rest = n & 0x7FFull;
-    mant += (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
-    // |v| = n 2^-lz = mant 2^(11 - lz): biased exponent 1086 - lz + k; a carry
-    // of the rounding into bit 53 moves into the exponent by the addition
-    const long long e = 1086 - lz + k;
-    return (long long)(neg | (((unsigned long long)(e - 1) << 52) + mant));
 }
 
 // One CTA: NTR transforms of length N of plane blockIdx.y.  COLS: columns

@@ -18,14 +18,18 @@
 // cell by cell with TwoSum (hi + lo), in chunk order, so the error of a cell
 // does not grow with the number of measurements that hit it.
 //
-// FP64 (k_grid_f64): whole bins (a split bin is processed by the CTA that
-// takes its first item), FP64 shared-memory atomics.  The kernel is bound by
-// FP64 instruction issue, so a warp takes several records at once
-// (taps64.cuh): six exponentials per record from one warp-wide pass, then a
-// group of G lanes per record, lane k scattering row k of the window; the
-// tile's pitch T + 2K + 1 puts the rows of one window in distinct banks.
+// FP64 (k_grid_f64): the same work items and partial-tile combination (in
+// FP64, chunk order).  The FP64 pipe issues at 1/64 of the integer rate, so
+// the weights are factorised (taps64.cuh: four exponentials per record, one
+// warp-wide pass for eight records) and the taps are summed as 64-bit
+// integers at an order-independent power-of-two scale per item (fixed64.cuh);
+// an item above kFixedMaxRecords records, or holding a NaN or an infinity,
+// sums in FP64 shared-memory atomics.  A group of G lanes takes a record, lane
+// k scattering row k of the window; the tile's pitch T + 2K + 1 puts the rows
+// of one window in distinct banks.
 #include <cuda_runtime.h>
 
+#include "fixed64.cuh"
 #include "taps64.cuh"
 #include "wsg_internal.cuh"
 
@@ -299,8 +303,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
             }
             __stcg(cell, make_float2(hr + lr, hi + li));
         }
+        if (tid == 0) a.b.done[bin] = 0u;   // rearmed for the next launch
     }
 }
+
+// Largest work item the FP64 gridder sums in fixed point: the bound below
+// costs bitlen(records) bits of the 62, so the error of a cell stays below
+// about 2^-49 of the item's largest value times the peak weight, whatever
+// the cancellation in the cell.  Larger items (whole bins when there is no
+// partial-tile buffer, or a chunk size raised above this) sum in FP64.
+constexpr unsigned kFixedMaxRecords = 4096;
 
 template <int T, int K>
 __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
@@ -309,37 +321,70 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
     constexpr int NT = P::NT;
     constexpr int PITCH = T + NT;
     constexpr int NW = kThreads / 32;
-    extern __shared__ double smd[];
-    double *sre = smd;
-    double *sim = smd + T * PITCH;
-    __shared__ unsigned s_item;
+    extern __shared__ long long smd[];
+    unsigned long long *sre = reinterpret_cast<unsigned long long *>(smd);
+    unsigned long long *sim = sre + T * PITCH;
+    __shared__ unsigned s_item, s_exp;
+    __shared__ int s_last;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / P::G, row = lane % P::G;
     const double2 *__restrict__ fr_all = reinterpret_cast<const double2 *>(a.r.frac);
     const double2 *__restrict__ val_all = reinterpret_cast<const double2 *>(a.r.val);
     double2 *grid = reinterpret_cast<double2 *>(a.grid);
+    double2 *parts = reinterpret_cast<double2 *>(a.partials);
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+    const unsigned split = a.b.split_size;
     double nt_u, t_v;
     taps64_consts<K>(lane, 0.5 / kRefPi, nt_u, t_v);
 
-    for (int i = tid; i < 2 * T * PITCH; i += kThreads) smd[i] = 0.0;
+    for (int i = tid; i < 2 * T * PITCH; i += kThreads) smd[i] = 0;
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_grid, 1u);
+        if (tid == 0) {
+            s_item = atomicAdd(&a.b.ctr->work_grid, 1u);
+            s_exp = 0u;
+        }
         __syncthreads();
         const unsigned item = s_item;
         if (item >= nitems) break;
         unsigned bin, chunk;
-        if (!work_item(a.b, item, nsplit, bin, chunk) || chunk != 0) continue;
+        if (!work_item(a.b, item, nsplit, bin, chunk)) continue;
+        // without a partial-tile buffer, the first item of a split bin takes
+        // the whole bin
+        if (!parts && chunk != 0) continue;
+        const bool is_split = parts && item < nsplit;
         int w, u0, v0;
         decode_bin(a.g, bin, w, u0, v0);
         const int tx = min(T, a.g.nx - u0);
         const int ty = min(T, a.g.ny - v0);
-        const unsigned off = a.b.off[bin];
-        const unsigned n = a.b.ntotal[bin];
+        const unsigned total = a.b.ntotal[bin];
+        const unsigned r0 = is_split ? chunk * split : 0u;
+        const unsigned r1 = is_split ? min(total, r0 + split) : total;
+        const unsigned off = a.b.off[bin] + r0;
+        const unsigned n = r1 - r0;
+
+        // The item's scale, from the largest exponent of its values (an
+        // order-independent bound): every |tap| <= norm * max|V| < 2^(e - 1024)
+        // and a cell takes at most n taps, so with
+        //   f = 64 - bitlen(n) - (e - 1022)
+        // a tap's value times 2^f is below 2^(62 - bitlen(n)) and every
+        // partial sum of a cell below 2^62.  An item holding a NaN or an
+        // infinity (e = 2047) sums in FP64 atomics instead, which propagate
+        // as the reference's do.
+        unsigned ex = 0u;
+        for (unsigned rr = tid; rr < n; rr += kThreads) {
+            const double2 v = __ldg(val_all + off + rr);
+            ex = max(ex, max(exp_field(v.x), exp_field(v.y)));
+        }
+        ex = __reduce_max_sync(0xFFFFFFFFu, ex);
+        if (lane == 0) atomicMax(&s_exp, ex);
+        __syncthreads();
+        const int e = (int)s_exp;
+        const bool fixed = e < 2047 && n <= kFixedMaxRecords;
+        const int f = min(64 - (32 - __clz((int)n)) - (e - 1022), 1020);
 
         for (unsigned base = warp * P::RE; base < n; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, n - base);
@@ -360,28 +405,85 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
                 const int y = (int)(cell >> 16) - 32768 - K + row;
                 const bool on = (unsigned)r < cnt && row < NT && (unsigned)y < (unsigned)ty;
                 const double au = gu * v.x, bu = gu * v.y;
+                if (fixed) {
+                    // tap = (gu V 2^f) (gv 2^62) / 2^64: the cell sums carry 2^(f-2)
+                    const Half64 ar = split64(to_fixed(__double_as_longlong(au), f));
+                    const Half64 ai = split64(to_fixed(__double_as_longlong(bu), f));
+                    const Half64 g = split64(to_fixed(__double_as_longlong(gv), 62));
 #pragma unroll
-                for (int j = 0; j < NT; j++) {
-                    const double tr = __shfl_sync(0xFFFFFFFFu, au, grp * P::G + j);
-                    const double ti = __shfl_sync(0xFFFFFFFFu, bu, grp * P::G + j);
-                    const int x = cu + j;
-                    if (on && (unsigned)x < (unsigned)tx) {
-                        atomicAdd(sre + y * PITCH + x, tr * gv);
-                        atomicAdd(sim + y * PITCH + x, ti * gv);
+                    for (int j = 0; j < NT; j++) {
+                        const int src = grp * P::G + j;
+                        const Half64 tr = {__shfl_sync(0xFFFFFFFFu, ar.h, src),
+                                           __shfl_sync(0xFFFFFFFFu, ar.l, src)};
+                        const Half64 ti = {__shfl_sync(0xFFFFFFFFu, ai.h, src),
+                                           __shfl_sync(0xFFFFFFFFu, ai.l, src)};
+                        const int x = cu + j;
+                        if (on && (unsigned)x < (unsigned)tx) {
+                            atomicAdd(sre + y * PITCH + x, (unsigned long long)mulhi_bal(tr, g));
+                            atomicAdd(sim + y * PITCH + x, (unsigned long long)mulhi_bal(ti, g));
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NT; j++) {
+                        const double tr = __shfl_sync(0xFFFFFFFFu, au, grp * P::G + j);
+                        const double ti = __shfl_sync(0xFFFFFFFFu, bu, grp * P::G + j);
+                        const int x = cu + j;
+                        if (on && (unsigned)x < (unsigned)tx) {
+                            atomicAdd(reinterpret_cast<double *>(sre + y * PITCH + x), tr * gv);
+                            atomicAdd(reinterpret_cast<double *>(sim + y * PITCH + x), ti * gv);
+                        }
                     }
                 }
             }
         }
         __syncthreads();
+        // write the interior (to the grid, or to this item's partial slot) and clear it
+        const size_t gbase = (size_t)w * a.g.ny;
+        const bool to_grid = !(is_split && chunk > 0);
+        double2 *slot = to_grid ? nullptr
+                                : parts + (size_t)(a.b.slot[bin] + chunk - 1) * (size_t)(T * T);
         for (int c = tid; c < T * T; c += kThreads) {
             const int y = c / T, x = c % T;
             const int idx = y * PITCH + x;
-            if (x < tx && y < ty)
-                grid[((size_t)w * a.g.ny + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x)] =
-                    make_double2(sre[idx], sim[idx]);
-            sre[idx] = 0.0;
-            sim[idx] = 0.0;
+            const long long br = (long long)sre[idx], bi = (long long)sim[idx];
+            const double2 v =
+                fixed ? make_double2(__longlong_as_double(from_fixed(br, 2 - f)),
+                                     __longlong_as_double(from_fixed(bi, 2 - f)))
+                      : make_double2(__longlong_as_double(br), __longlong_as_double(bi));
+            sre[idx] = 0ull;
+            sim[idx] = 0ull;
+            if (to_grid) {
+                if (x < tx && y < ty)
+                    grid[(gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x)] = v;
+            } else {
+                __stcg(slot + c, v);
+            }
         }
+        if (!is_split) continue;
+        // split bin: the CTA finishing its last item adds the partials in
+        // chunk order and rearms the bin's counter for the next launch
+        __threadfence();
+        __syncthreads();
+        const unsigned nchunks = (total + split - 1) / split;
+        if (tid == 0) s_last = atomicAdd(&a.b.done[bin], 1u) == nchunks - 1;
+        __syncthreads();
+        if (!s_last) continue;
+        __threadfence();
+        const double2 *src = parts + (size_t)a.b.slot[bin] * (size_t)(T * T);
+        for (int c = tid; c < T * T; c += kThreads) {
+            const int y = c / T, x = c % T;
+            if (x >= tx || y >= ty) continue;
+            double2 *cell = grid + (gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x);
+            double2 acc = __ldcg(cell);
+            for (unsigned q = 1; q < nchunks; q++) {
+                const double2 p = __ldcg(src + (size_t)(q - 1) * (size_t)(T * T) + c);
+                acc.x += p.x;
+                acc.y += p.y;
+            }
+            __stcg(cell, acc);
+        }
+        if (tid == 0) a.b.done[bin] = 0u;
     }
 }
 
