@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "fixed64.cuh"
 #include "wsg_internal.cuh"
 
 namespace wsg {
@@ -97,6 +98,115 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
     const float z = s - hi;
     lo += (hi - (s - z)) + (x - z);
     hi = s;
+}
+
+// ---- FP64 form on the integer pipe --------------------------------------
+//
+// The phase of plane w at a pixel is the cycle count (wmin + w dw) t kappa
+// (kappa = PI / pi, the reference's PI), taken modulo 1 as a Q64 fraction.
+// Its cosine and sine come from a 256-entry table of e^{2 pi i k / 256} (Q62,
+// built per CTA with FP64 sincospi) and Taylor series of the remaining angle
+// (below 2 pi / 256, terms to the 7th power, truncation below 1e-17);
+// the planes' phasors then follow by the recurrence e_{w+1} = e_w e_step in
+// Q62.  The plane values enter as 53-bit mantissas with a shared exponent
+// per complex value, the products are balanced 32-bit-half products, and
+// the sum over planes is block floating point (a 64-bit pair with one
+// exponent, realigned when a larger term arrives), so about 51 bits of the
+// largest term are kept.  No FP64 instruction runs per (pixel, plane).
+
+// (a * b) >> 62, exact floor, for signed a and b.
+__device__ __forceinline__ long long q62mul(long long a, long long b)
+{
+    const long long hi = __mul64hi(a, b);
+    const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
+    return (hi << 2) | (long long)(lo >> 62);
+}
+
+// frac(c) * 2^64 for the FP64 value c (bits below 2^-64 truncated).
+__device__ __forceinline__ unsigned long long cycles_q64(double c)
+{
+    const long long bits = __double_as_longlong(c);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long m =
+        (unsigned long long)(bits & 0xFFFFFFFFFFFFFll) | (e ? 0x10000000000000ull : 0ull);
+    const int k = max(e, 1) - 1075 + 64;        // c 2^64 = m 2^k
+    unsigned long long q;
+    if (k >= 64 || k <= -64) q = 0ull;
+    else if (k >= 0) q = m << k;
+    else q = m >> (-k);
+    return bits < 0 ? 0ull - q : q;
+}
+
+// e^{2 pi i q / 2^64} in Q62; tab[k] = e^{2 pi i k / 256} in Q62.
+__device__ __forceinline__ longlong2 cis_q62(unsigned long long q, const longlong2 *tab)
+{
+    constexpr long long ONE = 1ll << 62;
+    constexpr long long PI_2 = 0x6487ED5110B4611All;   // pi/2 in Q62
+    const longlong2 t = tab[q >> 56];
+    const unsigned long long r = q & 0x00FFFFFFFFFFFFFFull;   // < 2^56
+    // d = 2 pi r / 2^64 in Q62 = r pi / 2
+    const long long d = (long long)__umul64hi(r << 2, (unsigned long long)PI_2);
+    const long long d2 = q62mul(d, d);
+    const long long d4 = q62mul(d2, d2);
+    const long long d6 = q62mul(d4, d2);
+    const long long c = ONE - (d2 >> 1) + d4 / 24 - d6 / 720;
+    const long long sp = ONE - d2 / 6 + d4 / 120 - d6 / 5040;
+    const long long sn = q62mul(d, sp);
+    return make_longlong2(q62mul(t.x, c) - q62mul(t.y, sn), q62mul(t.y, c) + q62mul(t.x, sn));
+}
+
+// The table, built by the CTA's first 256 threads (needs a barrier after).
+__device__ __forceinline__ void cis_table(longlong2 *tab)
+{
+    if (threadIdx.x < 256) {
+        double sn, cs;
+        sincospi((double)threadIdx.x / 128.0, &sn, &cs);
+        const double q = 4611686018427387904.0;   // 2^62
+        tab[threadIdx.x] = make_longlong2(__double2ll_rn(cs * q), __double2ll_rn(sn * q));
+    }
+}
+
+// a * b / 2^62 for Q62 phasors (|a|, |b| <= 1).
+__device__ __forceinline__ longlong2 cmul_q62(longlong2 a, longlong2 b)
+{
+    const Half64 ar = split64(a.x), ai = split64(a.y), br = split64(b.x), bi = split64(b.y);
+    return make_longlong2((mulhi_bal(ar, br) - mulhi_bal(ai, bi)) << 2,
+                          (mulhi_bal(ar, bi) + mulhi_bal(ai, br)) << 2);
+}
+
+// A complex FP64 value as signed 53-bit mantissas with one exponent:
+// value = m * 2^(e - 1075).  e = 2047 marks NaN or infinity.
+struct Mant2 {
+    long long r, i;
+    int e;
+};
+
+__device__ __forceinline__ Mant2 to_mant2(double2 v)
+{
+    const long long br = __double_as_longlong(v.x), bi = __double_as_longlong(v.y);
+    const int er = (int)((br >> 52) & 0x7FF), ei = (int)((bi >> 52) & 0x7FF);
+    long long mr = (br & 0xFFFFFFFFFFFFFll) | (er ? 0x10000000000000ll : 0ll);
+    long long mi = (bi & 0xFFFFFFFFFFFFFll) | (ei ? 0x10000000000000ll : 0ll);
+    const int xr = max(er, 1), xi = max(ei, 1), e = max(xr, xi);
+    const int sr = e - xr, si = e - xi;
+    mr = sr >= 63 ? 0 : (sr ? ((mr >> (sr - 1)) + 1) >> 1 : mr);
+    mi = si >= 63 ? 0 : (si ? ((mi >> (si - 1)) + 1) >> 1 : mi);
+    return {br < 0 ? -mr : mr, bi < 0 ? -mi : mi, max(er, ei) == 2047 ? 2047 : e};
+}
+
+// x >> k rounded, k >= 0 (0 for k >= 63).
+__device__ __forceinline__ long long shr_rn(long long x, int k)
+{
+    return k >= 63 ? 0 : (k ? ((x >> (k - 1)) + 1) >> 1 : x);
+}
+
+// v 2^k as FP64, flushing results below the normal range to zero.
+__device__ __forceinline__ double fixed_to_f64(long long v, int k)
+{
+    if (v == 0) return 0.0;
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    if (1086 - __clzll((long long)a) + k < 1) return 0.0;
+    return __longlong_as_double(from_fixed(v, k));
 }
 
 constexpr float kTwoPiF = 6.28318530717958647692f;
@@ -173,40 +283,53 @@ k_wcorrect_f64(WcParams p, const double *__restrict__ sinx, const double *__rest
                const double2 *__restrict__ planes, double2 *__restrict__ image,
                double *__restrict__ image_re, double *__restrict__ image_im, double scale)
 {
+    __shared__ longlong2 tab[256];
+    cis_table(tab);
+    __syncthreads();
     const long long npix = (long long)p.xaxis * p.yaxis;
     const bool phase = p.phase_on && p.planes > 1;
     const double dw = (p.wmax - p.wmin) / (double)p.planes;
     const double dwnorm = dw / (p.wmax - p.wmin);
+    const double kappa = kRefPi / 3.141592653589793238462643383279502884;
     for (long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x; pix < npix;
          pix += (long long)gridDim.x * blockDim.x) {
-        double sr = 0.0, si = 0.0;
+        double s = 1.0;
+        longlong2 ph = make_longlong2(1ll << 62, 0), step = ph;
         if (phase) {
             const int iu = (int)(pix % p.xaxis);
             const int iv = (int)(pix / p.xaxis);
-            const double s = pixel_cosine(sinx[iu], siny[iv]);
+            s = pixel_cosine(sinx[iu], siny[iv]);
             const double t = s - 1.0;
-            double er, ei, rr, ri;
-            sincos(2.0 * kRefPi * p.wmin * t, &ei, &er);
-            sincos(2.0 * kRefPi * dw * t, &ri, &rr);
-            for (int w = 0; w < p.planes; w++) {
-                const double2 g = __ldcs(planes + (size_t)w * npix + pix);
-                sr += g.x * er - g.y * ei;
-                si += g.x * ei + g.y * er;
-                const double nr = er * rr - ei * ri;
-                ei = er * ri + ei * rr;
-                er = nr;
+            ph = cis_q62(cycles_q64((p.wmin * t) * kappa), tab);
+            step = cis_q62(cycles_q64((dw * t) * kappa), tab);
+        }
+        // sum_w plane_w e_w, block floating point: (ar, ai) 2^(ea - 1075 + 2)
+        long long ar = 0, ai = 0;
+        int ea = 0;
+        bool bad = false;
+        for (int w = 0; w < p.planes; w++) {
+            const Mant2 g = to_mant2(__ldcs(planes + (size_t)w * npix + pix));
+            bad |= g.e == 2047;
+            const Half64 gr = split64(g.r), gi = split64(g.i);
+            const Half64 pr = split64(ph.x), pi = split64(ph.y);
+            const long long tr = mulhi_bal(gr, pr) - mulhi_bal(gi, pi);
+            const long long ti = mulhi_bal(gr, pi) + mulhi_bal(gi, pr);
+            if (g.e > ea) {
+                ar = shr_rn(ar, g.e - ea);
+                ai = shr_rn(ai, g.e - ea);
+                ea = g.e;
             }
-            const double amp = dwnorm * s * scale;
-            sr *= amp;
-            si *= amp;
+            ar += shr_rn(tr, ea - g.e);
+            ai += shr_rn(ti, ea - g.e);
+            if (phase) ph = cmul_q62(ph, step);
+        }
+        double sr, si;
+        if (bad || !(s == s)) {
+            sr = si = __longlong_as_double(0x7FF8000000000000ll);
         } else {
-            for (int w = 0; w < p.planes; w++) {
-                const double2 g = __ldcs(planes + (size_t)w * npix + pix);
-                sr += g.x;
-                si += g.y;
-            }
-            sr *= scale;
-            si *= scale;
+            const double amp = phase ? dwnorm * s * scale : scale;
+            sr = fixed_to_f64(ar, ea - 1075 + 2) * amp;
+            si = fixed_to_f64(ai, ea - 1075 + 2) * amp;
         }
         if (image) image[pix] = make_double2(sr, si);
         if (image_re) image_re[pix] = sr;
@@ -218,38 +341,49 @@ __global__ void __launch_bounds__(256)
 k_wcorrect_adj_f64(WcParams p, const double *__restrict__ sinx, const double *__restrict__ siny,
                    const double2 *__restrict__ image, double2 *__restrict__ planes, double scale)
 {
+    __shared__ longlong2 tab[256];
+    cis_table(tab);
+    __syncthreads();
     const long long npix = (long long)p.xaxis * p.yaxis;
     const bool phase = p.phase_on && p.planes > 1;
     const double dw = (p.wmax - p.wmin) / (double)p.planes;
     const double dwnorm = dw / (p.wmax - p.wmin);
+    const double kappa = kRefPi / 3.141592653589793238462643383279502884;
     for (long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x; pix < npix;
          pix += (long long)gridDim.x * blockDim.x) {
         const double2 im = image[pix];
-        if (phase) {
-            const int iu = (int)(pix % p.xaxis);
-            const int iv = (int)(pix / p.xaxis);
-            const double s = pixel_cosine(sinx[iu], siny[iv]);
-            const double t = s - 1.0;
-            const double amp = dwnorm * s * scale;
-            if (!(amp == amp)) {  // pixel where the forward is NaN: excluded
-                for (int w = 0; w < p.planes; w++)
-                    __stcs(planes + (size_t)w * npix + pix, make_double2(0.0, 0.0));
-                continue;
-            }
-            const double xr = im.x * amp, xi = im.y * amp;
-            double er, ei, rr, ri;
-            sincos(2.0 * kRefPi * p.wmin * t, &ei, &er);
-            sincos(2.0 * kRefPi * dw * t, &ri, &rr);
-            for (int w = 0; w < p.planes; w++) {
-                __stcs(planes + (size_t)w * npix + pix,
-                       make_double2(er * xr + ei * xi, er * xi - ei * xr));
-                const double nr = er * rr - ei * ri;
-                ei = er * ri + ei * rr;
-                er = nr;
-            }
-        } else {
+        if (!phase) {
             const double2 v = make_double2(im.x * scale, im.y * scale);
             for (int w = 0; w < p.planes; w++) __stcs(planes + (size_t)w * npix + pix, v);
+            continue;
+        }
+        const int iu = (int)(pix % p.xaxis);
+        const int iv = (int)(pix / p.xaxis);
+        const double s = pixel_cosine(sinx[iu], siny[iv]);
+        const double t = s - 1.0;
+        const double amp = dwnorm * s * scale;
+        if (!(amp == amp)) {  // pixel where the forward is NaN: excluded
+            for (int w = 0; w < p.planes; w++)
+                __stcs(planes + (size_t)w * npix + pix, make_double2(0.0, 0.0));
+            continue;
+        }
+        longlong2 ph = cis_q62(cycles_q64((p.wmin * t) * kappa), tab);
+        const longlong2 step = cis_q62(cycles_q64((dw * t) * kappa), tab);
+        const Mant2 x = to_mant2(make_double2(im.x * amp, im.y * amp));
+        const Half64 xr = split64(x.r), xi = split64(x.i);
+        const int k = x.e - 1075 + 2;
+        for (int w = 0; w < p.planes; w++) {
+            // conj(e_w) x
+            const Half64 pr = split64(ph.x), pi = split64(ph.y);
+            const long long orr = mulhi_bal(xr, pr) + mulhi_bal(xi, pi);
+            const long long oi = mulhi_bal(xi, pr) - mulhi_bal(xr, pi);
+            double2 o;
+            if (x.e == 2047)
+                o.x = o.y = __longlong_as_double(0x7FF8000000000000ll);
+            else
+                o = make_double2(fixed_to_f64(orr, k), fixed_to_f64(oi, k));
+            __stcs(planes + (size_t)w * npix + pix, o);
+            ph = cmul_q62(ph, step);
         }
     }
 }
