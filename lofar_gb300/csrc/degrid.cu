@@ -260,6 +260,8 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
     const unsigned nitems = nsplit + (unsigned)a.g.nbins;
     double nt_u, t_v;
     taps64_consts<K>(lane, 0.5 / kRefPi, nt_u, t_v);
+    const long long nt_uq = to_fixed(__double_as_longlong(nt_u), 62);
+    const long long t_vq = to_fixed(__double_as_longlong(t_v), 62);
 
     for (;;) {
         __syncthreads();
@@ -308,11 +310,10 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
         for (unsigned base = p0 + warp * P::RE; base < p1; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, p1 - base);
             const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
+            const Exps64Q EQ = taps64_exps_q62(E);
 #pragma unroll
             for (int s = 0; s < P::SUB; s++) {
                 const int r = s * P::R + grp;
-                double gu, gv;
-                taps64_factors<K>(E, r, lane, nt_u, t_v, gu, gv);
                 unsigned cell = 0, idx = 0;
                 if ((unsigned)r < cnt) {
                     cell = __ldg(a.r.cell + off + base + r);
@@ -327,8 +328,10 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
                 if (fixed) {
                     // sum_j (cell 2^s)(gu 2^62) / 2^64, times (gv 2^62) / 2^64:
                     // the result carries 2^(s-4); partial sums stay below 2^63
-                    const Half64 u = split64(to_fixed(__double_as_longlong(gu), 62));
-                    const Half64 g = split64(to_fixed(__double_as_longlong(gv), 62));
+                    long long guq, gvq;
+                    taps64_factors_q62<K>(EQ, r, lane, nt_uq, t_vq, guq, gvq);
+                    const Half64 u = split64(guq);
+                    const Half64 g = split64(gvq);
                     long long sr = 0, si = 0;
 #pragma unroll
                     for (int j = 0; j < NT; j++) {
@@ -352,6 +355,8 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
                     o = make_double2(__longlong_as_double(from_fixed(sr, 4 - sc)),
                                      __longlong_as_double(from_fixed(si, 4 - sc)));
                 } else {
+                    double gu, gv;
+                    taps64_factors<K>(E, r, lane, nt_u, t_v, gu, gv);
                     double sr = 0.0, si = 0.0;
 #pragma unroll
                     for (int j = 0; j < NT; j++) {

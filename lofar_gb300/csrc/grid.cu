@@ -338,6 +338,8 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
     const unsigned split = a.b.split_size;
     double nt_u, t_v;
     taps64_consts<K>(lane, 0.5 / kRefPi, nt_u, t_v);
+    const long long nt_uq = to_fixed(__double_as_longlong(nt_u), 62);
+    const long long t_vq = to_fixed(__double_as_longlong(t_v), 62);
 
     for (int i = tid; i < 2 * T * PITCH; i += kThreads) smd[i] = 0;
 
@@ -369,11 +371,11 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         // The item's scale, from the largest exponent of its values (an
         // order-independent bound): every |tap| <= norm * max|V| < 2^(e - 1024)
         // and a cell takes at most n taps, so with
-        //   f = 64 - bitlen(n) - (e - 1022)
+        //   f = 64 - max(bitlen(n), 4) - (e - 1022)
         // a tap's value times 2^f is below 2^(62 - bitlen(n)) and every
-        // partial sum of a cell below 2^62.  An item holding a NaN or an
-        // infinity (e = 2047) sums in FP64 atomics instead, which propagate
-        // as the reference's do.
+        // partial sum of a cell below 2^62; the values enter as V 2^(f+2),
+        // below 2^62.  An item holding a NaN or an infinity (e = 2047) sums in
+        // FP64 atomics instead, which propagate as the reference's do.
         unsigned ex = 0u;
         for (unsigned rr = tid; rr < n; rr += kThreads) {
             const double2 v = __ldg(val_all + off + rr);
@@ -384,16 +386,15 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         __syncthreads();
         const int e = (int)s_exp;
         const bool fixed = e < 2047 && n <= kFixedMaxRecords;
-        const int f = min(64 - (32 - __clz((int)n)) - (e - 1022), 1020);
+        const int f = min(64 - max(32 - __clz((int)n), 4) - (e - 1022), 1018);
 
         for (unsigned base = warp * P::RE; base < n; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, n - base);
             const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
+            const Exps64Q EQ = taps64_exps_q62(E);
 #pragma unroll
             for (int s = 0; s < P::SUB; s++) {
                 const int r = s * P::R + grp;
-                double gu, gv;
-                taps64_factors<K>(E, r, lane, nt_u, t_v, gu, gv);
                 unsigned cell = 0;
                 double2 v = make_double2(0.0, 0.0);
                 if ((unsigned)r < cnt) {
@@ -404,12 +405,17 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
                 const int cu = (int)(cell & 0xFFFFu) - 32768 - K;
                 const int y = (int)(cell >> 16) - 32768 - K + row;
                 const bool on = (unsigned)r < cnt && row < NT && (unsigned)y < (unsigned)ty;
-                const double au = gu * v.x, bu = gu * v.y;
                 if (fixed) {
-                    // tap = (gu V 2^f) (gv 2^62) / 2^64: the cell sums carry 2^(f-2)
-                    const Half64 ar = split64(to_fixed(__double_as_longlong(au), f));
-                    const Half64 ai = split64(to_fixed(__double_as_longlong(bu), f));
-                    const Half64 g = split64(to_fixed(__double_as_longlong(gv), 62));
+                    long long guq, gvq;
+                    taps64_factors_q62<K>(EQ, r, lane, nt_uq, t_vq, guq, gvq);
+                    // (V 2^(f+2)) (gu 2^62) / 2^64 = gu V 2^f, then times
+                    // (gv 2^62) / 2^64: the cell sums carry 2^(f-2)
+                    const Half64 gq = split64(guq);
+                    const Half64 ar =
+                        split64(mulhi_bal(split64(to_fixed(__double_as_longlong(v.x), f + 2)), gq));
+                    const Half64 ai =
+                        split64(mulhi_bal(split64(to_fixed(__double_as_longlong(v.y), f + 2)), gq));
+                    const Half64 g = split64(gvq);
 #pragma unroll
                     for (int j = 0; j < NT; j++) {
                         const int src = grp * P::G + j;
@@ -424,6 +430,9 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
                         }
                     }
                 } else {
+                    double gu, gv;
+                    taps64_factors<K>(E, r, lane, nt_u, t_v, gu, gv);
+                    const double au = gu * v.x, bu = gu * v.y;
 #pragma unroll
                     for (int j = 0; j < NT; j++) {
                         const double tr = __shfl_sync(0xFFFFFFFFu, au, grp * P::G + j);

@@ -22,6 +22,8 @@
 
 #include <cuda_runtime.h>
 
+#include "fixed64.cuh"
+
 namespace wsg {
 
 template <int K> struct Taps64 {
@@ -96,6 +98,54 @@ __device__ __forceinline__ void taps64_factors(const Exps64 &E, int r, int lane,
     }
     gu = nt_u * au * pu;
     gv = t_v * av * pv;
+}
+
+// Integer form of the factors: Q62 values of gu and gv (zero past the
+// window).  The exponential pass's values are converted to Q62 on their own
+// lanes; each ladder starts from exp(-m^2/2) exp(-c^2/2) and multiplies by
+// exp(-+c) |m| times, and every partial product exp(-m^2/2) exp(|i c|) with
+// i <= |m| stays below 1 (|c| <= 1/2), so nothing leaves Q62.  A product is
+// rounded to within 4 units of 2^-62.
+struct Exps64Q {
+    long long e, inv;   // Q62
+};
+
+__device__ __forceinline__ Exps64Q taps64_exps_q62(const Exps64 &E)
+{
+    return {to_fixed(__double_as_longlong(E.e), 62), to_fixed(__double_as_longlong(E.inv), 62)};
+}
+
+__device__ __forceinline__ long long q62mul_bal(long long a, long long b)
+{
+    return mulhi_bal(split64(a), split64(b)) << 2;
+}
+
+template <int K>
+__device__ __forceinline__ void taps64_factors_q62(const Exps64Q &E, int r, int lane,
+                                                   long long nt_u, long long t_v, long long &gu,
+                                                   long long &gv)
+{
+    using P = Taps64<K>;
+    const int m = lane % P::G - K;
+    const int am = m < 0 ? -m : m;
+    const int q = 4 * r;
+    const long long au = __shfl_sync(0xFFFFFFFFu, E.e, q);
+    const long long bu_p = __shfl_sync(0xFFFFFFFFu, E.e, q + 1);
+    const long long bu_n = __shfl_sync(0xFFFFFFFFu, E.inv, q + 1);
+    const long long av = __shfl_sync(0xFFFFFFFFu, E.e, q + 2);
+    const long long bv_p = __shfl_sync(0xFFFFFFFFu, E.e, q + 3);
+    const long long bv_n = __shfl_sync(0xFFFFFFFFu, E.inv, q + 3);
+    const long long bu = m > 0 ? bu_p : bu_n;
+    const long long bv = m > 0 ? bv_p : bv_n;
+    gu = q62mul_bal(nt_u, au);
+    gv = q62mul_bal(t_v, av);
+#pragma unroll
+    for (int t = 1; t <= K; t++) {
+        if (t <= am) {
+            gu = q62mul_bal(gu, bu);
+            gv = q62mul_bal(gv, bv);
+        }
+    }
 }
 
 }  // namespace wsg
