@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
         for (unsigned base = p0 + warp * P::RE; base < p1; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, p1 - base);
             const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
-            const Exps64Q EQ = taps64_exps_q62(E);
+            const Exps64Q EQ = taps64_exps_q60(E);
 #pragma unroll
             for (int s = 0; s < P::SUB; s++) {
                 const int r = s * P::R + grp;
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
                     // sum_j (cell 2^s)(gu 2^62) / 2^64, times (gv 2^62) / 2^64:
                     // the result carries 2^(s-4); partial sums stay below 2^63
                     long long guq, gvq;
-                    taps64_factors_q62<K>(EQ, r, lane, nt_uq, t_vq, guq, gvq);
+                    taps64_factors_q<K>(EQ, r, lane, nt_uq, t_vq, guq, gvq);
                     const Half64 u = split64(guq);
                     const Half64 g = split64(gvq);
                     long long sr = 0, si = 0;

@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         for (unsigned base = warp * P::RE; base < n; base += NW * P::RE) {
             const unsigned cnt = min((unsigned)P::RE, n - base);
             const Exps64 E = taps64_exps(fr_all + off + base, cnt, lane);
-            const Exps64Q EQ = taps64_exps_q62(E);
+            const Exps64Q EQ = taps64_exps_q60(E);
 #pragma unroll
             for (int s = 0; s < P::SUB; s++) {
                 const int r = s * P::R + grp;
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
                 const bool on = (unsigned)r < cnt && row < NT && (unsigned)y < (unsigned)ty;
                 if (fixed) {
                     long long guq, gvq;
-                    taps64_factors_q62<K>(EQ, r, lane, nt_uq, t_vq, guq, gvq);
+                    taps64_factors_q<K>(EQ, r, lane, nt_uq, t_vq, guq, gvq);
                     // (V 2^(f+2)) (gu 2^62) / 2^64 = gu V 2^f, then times
                     // (gv 2^62) / 2^64: the cell sums carry 2^(f-2)
                     const Half64 gq = split64(guq);

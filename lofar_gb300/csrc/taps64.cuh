@@ -101,27 +101,30 @@ __device__ __forceinline__ void taps64_factors(const Exps64 &E, int r, int lane,
 }
 
 // Integer form of the factors: Q62 values of gu and gv (zero past the
-// window).  The exponential pass's values are converted to Q62 on their own
-// lanes; each ladder starts from exp(-m^2/2) exp(-c^2/2) and multiplies by
-// exp(-+c) |m| times, and every partial product exp(-m^2/2) exp(|i c|) with
-// i <= |m| stays below 1 (|c| <= 1/2), so nothing leaves Q62.  A product is
-// rounded to within 4 units of 2^-62.
+// window).  The reference's cell is pos truncated toward zero, so frac lies
+// in (-1, 1), c in (-1/2, 3/2), and the exponential pass's values reach
+// e^{3/2}; they are converted to Q60 (below 8) on their own lanes.  Each
+// ladder starts from exp(-m^2/2) exp(-c^2/2) and multiplies by exp(-+c) |m|
+// times; every partial product exp(-(m^2 + c^2 - 2|i c|)/2), i <= |m|, is at
+// most 1, so gu and gv stay in Q62.  A product is rounded to within 16 units
+// of 2^-62.
 struct Exps64Q {
-    long long e, inv;   // Q62
+    long long e, inv;   // Q60
 };
 
-__device__ __forceinline__ Exps64Q taps64_exps_q62(const Exps64 &E)
+__device__ __forceinline__ Exps64Q taps64_exps_q60(const Exps64 &E)
 {
-    return {to_fixed(__double_as_longlong(E.e), 62), to_fixed(__double_as_longlong(E.inv), 62)};
+    return {to_fixed(__double_as_longlong(E.e), 60), to_fixed(__double_as_longlong(E.inv), 60)};
 }
 
-__device__ __forceinline__ long long q62mul_bal(long long a, long long b)
+// (a b) >> 60 for a in Q62 and b in Q60 (b below 2^62.6).
+__device__ __forceinline__ long long q60mul_bal(long long a, long long b)
 {
-    return mulhi_bal(split64(a), split64(b)) << 2;
+    return mulhi_bal(split64(a), split64(b)) << 4;
 }
 
 template <int K>
-__device__ __forceinline__ void taps64_factors_q62(const Exps64Q &E, int r, int lane,
+__device__ __forceinline__ void taps64_factors_q(const Exps64Q &E, int r, int lane,
                                                    long long nt_u, long long t_v, long long &gu,
                                                    long long &gv)
 {
@@ -137,13 +140,13 @@ __device__ __forceinline__ void taps64_factors_q62(const Exps64Q &E, int r, int 
     const long long bv_n = __shfl_sync(0xFFFFFFFFu, E.inv, q + 3);
     const long long bu = m > 0 ? bu_p : bu_n;
     const long long bv = m > 0 ? bv_p : bv_n;
-    gu = q62mul_bal(nt_u, au);
-    gv = q62mul_bal(t_v, av);
+    gu = q60mul_bal(nt_u, au);
+    gv = q60mul_bal(t_v, av);
 #pragma unroll
     for (int t = 1; t <= K; t++) {
         if (t <= am) {
-            gu = q62mul_bal(gu, bu);
-            gv = q62mul_bal(gv, bv);
+            gu = q60mul_bal(gu, bu);
+            gv = q60mul_bal(gv, bv);
         }
     }
 }

@@ -126,3 +126,32 @@ def test_fp64_degrid_nan_cell_propagates(gpu):
     # imaginary part of every output whose window holds the cell NaN
     assert np.isnan(ref[:, 1]).any() and not np.isnan(ref[:, 0]).any()
     assert _cmp_finite(out, ref) <= 1e-12
+
+
+def test_fp64_negative_coordinates(gpu):
+    """The reference's cell is pos truncated toward zero, so a measurement just
+    below u = 0 or v = 0 has a fraction in (-1, 0] and its window reaches onto
+    the grid from outside: the factorised weights then take exp(c) up to
+    e^1.5.  Grid and degrid match the oracle."""
+    import torch
+    from lofar_gb300 import Plan
+    o = _obs(seed=14)
+    rng = np.random.default_rng(15)
+    k = 3000
+    uu = np.concatenate([o.uu, rng.uniform(-3.0 / NX, 0.0, k), rng.uniform(0.2, 0.8, k)])
+    vv = np.concatenate([o.vv, rng.uniform(0.2, 0.8, k), rng.uniform(-3.0 / NX, 0.0, k)])
+    ww = np.concatenate([o.ww, rng.uniform(0.0, 0.99, 2 * k)])
+    vr = np.concatenate([o.vis_real, rng.standard_normal(2 * k).astype(np.float32)])
+    vi = np.concatenate([o.vis_img, rng.standard_normal(2 * k).astype(np.float32)])
+    wt = np.concatenate([o.weight, np.ones(2 * k, np.float32)])
+    ref = O.wstack(uu, vv, ww, vr, vi, wt, **KW)
+    p = Plan(NX, NX, PLANES, SUPPORT, precision="fp64")
+    p.bin(uu, vv, ww, vr, vi, wt)
+    g = torch.view_as_real(p.grid()).cpu().numpy()
+    assert _cmp_finite(g, ref) <= 1e-12
+    gin = np.random.default_rng(16).standard_normal((PLANES, NX, NX, 2))
+    dref = O.degrid(uu, vv, ww, gin, **KW)
+    gt = torch.view_as_complex(torch.as_tensor(np.ascontiguousarray(gin))).cuda()
+    out = torch.view_as_real(p.degrid(gt)).cpu().numpy()
+    p.close()
+    assert _cmp_finite(out, dref) <= 1e-12
