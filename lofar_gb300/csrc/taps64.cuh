@@ -1,19 +1,20 @@
-// FP64 Gaussian tap weights for the FP64 gridder and degridder.
+// Gaussian tap weights of the FP64 gridder and degridder.
 //
-// On this part an FP64 instruction issues at a small fraction of the FP32
-// rate, so the FP64 kernels are bound by the number of FP64 warp instructions
-// per record, not by memory.  The weights of the reference's kernel
-// (w-stacking.cu:80-92: norm * exp(-(du^2 + dv^2) / 2), du = i + 0.5 - pos)
-// are evaluated per axis as
+// On this part an FP64 instruction issues at 1/64 of the FP32 and integer
+// rates, so the weights of the reference's kernel (w-stacking.cu:80-92:
+// norm * exp(-(du^2 + dv^2) / 2), du = i + 0.5 - pos) are evaluated per axis
+// as
 //     exp(-(m + c)^2 / 2) = exp(-m^2 / 2) * exp(-c^2 / 2) * exp(-c)^m,
 // with c = 0.5 - frac (frac the record's offset inside its cell) and
 // m = -K..K the tap's offset from the cell; for m < 0, exp(-c)^m is taken as
 // (1 / exp(-c))^|m|.  A record needs four exponentials (two per axis)
-// instead of 2(2K+1), so one warp-wide exponential serves eight records:
-// lane q of the pass computes value q % 4 of record q / 4, and a warp-wide
-// reciprocal follows.  The factors exp(-m^2/2) are per-lane constants, and
-// the powers take K multiplies.  The rounding differs from the direct form
-// by a few units in the last place (at most K + 5 roundings per factor).
+// instead of 2(2K+1), so one warp-wide FP64 exponential serves eight
+// records: lane q of the pass computes value q % 4 of record q / 4, and a
+// warp-wide reciprocal follows.  That pass is the only FP64 arithmetic of
+// the fixed-point kernels: the factors exp(-m^2/2) are per-lane constants
+// and the K-step power ladders run in Q62 integers (taps64_factors_q).  The
+// FP64 ladders (taps64_factors) serve the FP64-atomic fallback.  The
+// rounding differs from the direct form by a few units in the last place.
 //
 // Tap layout: a group of G lanes (G = 4, 8 or 16, at least 2K+1) takes one
 // record, lane i of the group holding the u-factor of column i and the
