@@ -1074,7 +1074,11 @@ def main():
                         "image_rel_max_err": f["image_rel_max"],
                         "nan_mask_equal": f["nan_mask_equal"],
                         "grid_plane_rel_rms_err_max": f["plane_rel_rms_max"],
-                        "stages_ms": {s: statistics.median(v) for s, v in f["per"].items() if v}}
+                        "stages_ms": {s: statistics.median(v) for s, v in f["per"].items() if v},
+                        # complex128 cube; the FP64 form runs its taps, FFT and
+                        # w-correction in 64-bit fixed point, so its stages are
+                        # bound by integer (and FP64 exponential) issue, not HBM
+                        "stages": roofline(f["per"], n, args.nx, args.planes, 16, peak, peak_kind)}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
     if not args.no_cpu and world >= 1:

@@ -60,3 +60,21 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.max_over_ranks(3.5, 1) == 3.5
     assert bench.whole_job_mvis(50_000_000, 1, 20.0) == pytest.approx(2500.0)
+
+
+def test_stage_roofline_arithmetic():
+    """bench.py's per-stage GB/s: algorithmic bytes over the median time, as a
+    fraction of the peak (complex64 and complex128 cubes)."""
+    import bench
+    per = {"bin": [1.0, 1.0, 9.0], "grid": [2.0], "fft_wcorrect": [4.0],
+           "wcorrect_adj_fft": [4.0], "degrid": [2.0]}
+    n, nx, planes = 1_000_000, 1024, 4
+    for sc in (8, 16):
+        st = bench.roofline(per, n, nx, planes, sc, 1000.0, "measured")
+        ab = bench.algorithmic_bytes(n, nx, nx, planes, sc)
+        g = st["gridding(bin+grid)"]
+        assert g["ms"] == 3.0 and g["bytes"] == ab["grid"]
+        assert g["gbs"] == pytest.approx(ab["grid"] / 3e-3 / 1e9)
+        assert st["degrid"]["frac"] == pytest.approx(ab["degrid"] / 2e-3 / 1e9 / 1000.0)
+    assert bench.algorithmic_bytes(n, nx, nx, planes, 16)["fft_wcorrect"] == \
+        2 * bench.algorithmic_bytes(n, nx, nx, planes, 8)["fft_wcorrect"]
