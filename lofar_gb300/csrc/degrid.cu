@@ -238,14 +238,18 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     }
 }
 
+// The FP64 degridder's CTA: 512 threads, so that the two CTAs whose
+// (T + 2K)^2 complex128 tiles fit an SM keep 32 warps resident.
+constexpr int kThreadsD64 = 512;
+
 template <int T, int K>
-__global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
+__global__ void __launch_bounds__(kThreadsD64, 2) k_degrid_f64(DegridArgs a)
 {
     using P = Taps64<K>;
     constexpr int NT = P::NT;
     constexpr int HW = T + 2 * K;      // tile + halo
     constexpr int SP = T + NT;         // smem pitch (== HW + 1)
-    constexpr int NW = kThreads / 32;
+    constexpr int NW = kThreadsD64 / 32;
     extern __shared__ unsigned char smraw[];
     double2 *tile = reinterpret_cast<double2 *>(smraw);
     int4 *tfix = reinterpret_cast<int4 *>(smraw);   // the same cells in fixed point
@@ -279,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
         const unsigned off = a.b.off[bin];
         const size_t plane = (size_t)w * a.g.ny;
         unsigned ex = 0u;
-        for (int i = tid; i < HW * HW; i += kThreads) {
+        for (int i = tid; i < HW * HW; i += kThreadsD64) {
             const int y = i / HW, x = i - (i / HW) * HW;
             const int gy = v0 - K + y, gx = u0 - K + x;
             double2 val = make_double2(0.0, 0.0);
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f64(DegridArgs a)
         const bool fixed = e < 2047;
         const int sc = min(61 - (e - 1022), 1020);
         if (fixed) {
-            for (int i = tid; i < HW * HW; i += kThreads) {
+            for (int i = tid; i < HW * HW; i += kThreadsD64) {
                 const int y = i / HW, x = i - (i / HW) * HW;
                 const double2 val = tile[y * SP + x];
                 const Half64 hr = split64(to_fixed(__double_as_longlong(val.x), sc));
@@ -480,7 +484,8 @@ int degrid_max_ctas_per_sm(int prec, int tile, int half)
         cudaSuccess)
         return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, k, prec == WSG_FP64 ? kThreadsD64 : kThreads, smem) != cudaSuccess)
         return 0;
     return nb;
 }
@@ -513,7 +518,7 @@ cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b, co
     DegridArgs a{g, b, r, grid, out};
     if (prec == WSG_FP64) {
         void *args[] = {&a};
-        return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
+        return cudaLaunchKernel(k, dim3(ctas), dim3(kThreadsD64), args, smem, s);
     }
     void *args[] = {&a, &m};
     return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);

@@ -314,13 +314,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
 // partial-tile buffer, or a chunk size raised above this) sum in FP64.
 constexpr unsigned kFixedMaxRecords = 4096;
 
+// The FP64 gridder's CTA: 512 threads, 64 registers each, two CTAs per SM
+// (32 warps; three 256-thread CTAs at 80 registers gave 24).
+constexpr int kThreadsG64 = 512;
+
 template <int T, int K>
-__global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
+__global__ void __launch_bounds__(kThreadsG64, 2) k_grid_f64(GridArgs a)
 {
     using P = Taps64<K>;
     constexpr int NT = P::NT;
     constexpr int PITCH = T + NT;
-    constexpr int NW = kThreads / 32;
+    constexpr int NW = kThreadsG64 / 32;
     extern __shared__ long long smd[];
     unsigned long long *sre = reinterpret_cast<unsigned long long *>(smd);
     unsigned long long *sim = sre + T * PITCH;
@@ -341,7 +345,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
     const long long nt_uq = to_fixed(__double_as_longlong(nt_u), 62);
     const long long t_vq = to_fixed(__double_as_longlong(t_v), 62);
 
-    for (int i = tid; i < 2 * T * PITCH; i += kThreads) smd[i] = 0;
+    for (int i = tid; i < 2 * T * PITCH; i += kThreadsG64) smd[i] = 0;
 
     for (;;) {
         __syncthreads();
@@ -377,7 +381,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         // below 2^62.  An item holding a NaN or an infinity (e = 2047) sums in
         // FP64 atomics instead, which propagate as the reference's do.
         unsigned ex = 0u;
-        for (unsigned rr = tid; rr < n; rr += kThreads) {
+        for (unsigned rr = tid; rr < n; rr += kThreadsG64) {
             const double2 v = __ldg(val_all + off + rr);
             ex = max(ex, max(exp_field(v.x), exp_field(v.y)));
         }
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         const bool to_grid = !(is_split && chunk > 0);
         double2 *slot = to_grid ? nullptr
                                 : parts + (size_t)(a.b.slot[bin] + chunk - 1) * (size_t)(T * T);
-        for (int c = tid; c < T * T; c += kThreads) {
+        for (int c = tid; c < T * T; c += kThreadsG64) {
             const int y = c / T, x = c % T;
             const int idx = y * PITCH + x;
             const long long br = (long long)sre[idx], bi = (long long)sim[idx];
@@ -480,7 +484,7 @@ __global__ void __launch_bounds__(kThreads) k_grid_f64(GridArgs a)
         if (!s_last) continue;
         __threadfence();
         const double2 *src = parts + (size_t)a.b.slot[bin] * (size_t)(T * T);
-        for (int c = tid; c < T * T; c += kThreads) {
+        for (int c = tid; c < T * T; c += kThreadsG64) {
             const int y = c / T, x = c % T;
             if (x >= tx || y >= ty) continue;
             double2 *cell = grid + (gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x);
@@ -542,7 +546,8 @@ int grid_max_ctas_per_sm(int prec, int tile, int half)
         cudaSuccess)
         return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, k, prec == WSG_FP64 ? kThreadsG64 : kThreads, smem) != cudaSuccess)
         return 0;
     return nb;
 }
@@ -557,7 +562,8 @@ cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b, cons
     if (e != cudaSuccess) return e;
     GridArgs a{g, b, r, grid, partials};
     void *args[] = {&a};
-    return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
+    return cudaLaunchKernel(k, dim3(ctas), dim3(prec == WSG_FP64 ? kThreadsG64 : kThreads), args,
+                            smem, s);
 }
 
 }  // namespace wsg
