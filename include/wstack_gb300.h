@@ -112,7 +112,10 @@ typedef enum {
 } wsg_status;
 
 typedef enum {
-    WSG_FP64 = 0,   /* FP64 grid, FFT and w-correction: the reference's arithmetic */
+    WSG_FP64 = 0,   /* FP64 grid, planes and image, within 1e-12 (grid, FFT) and
+                       1e-11 (image) of the reference's FP64 arithmetic; the
+                       taps, the FFT of power-of-two grids and the w-correction
+                       run in 64-bit fixed point inside */
     WSG_FP32C = 1   /* complex64 grid with compensated (two-float) tile
                        accumulation; FP64-exact coordinates and phase argument */
 } wsg_precision;

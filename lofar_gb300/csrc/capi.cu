@@ -136,7 +136,7 @@ int wsg::plan_configure(wsg_plan *p)
     const char *fft_env = getenv("WSTACK_GB300_FFT");
     p->fused = p->prec == WSG_FP32C && fft_fused_supported(p->nx, p->ny, p->tile) &&
                !(fft_env && strcmp(fft_env, "cufft") == 0);
-    p->fft64 = p->prec == WSG_FP64 && fft64_supported(p->nx, p->ny) &&
+    p->fft64 = p->prec == WSG_FP64 && fft64_supported(p->nx, p->ny, p->cube_planes()) &&
                !(fft_env && strcmp(fft_env, "cufft") == 0);
     p->masks_valid = false;
     p->ctas_grid = p->ctas_user > 0 ? p->ctas_user : og * sms;
@@ -1007,7 +1007,8 @@ int legacy_fft(const double *in, double *out, int nx, int ny, int nplanes)
     const long long npix = (long long)nx * ny;
     const size_t bytes = sizeof(double2) * (size_t)npix * nplanes;
     const char *fft_env = getenv("WSTACK_GB300_FFT");
-    const bool int_fft = fft64_supported(nx, ny) && !(fft_env && strcmp(fft_env, "cufft") == 0);
+    const bool int_fft =
+        fft64_supported(nx, ny, nplanes) && !(fft_env && strcmp(fft_env, "cufft") == 0);
     if (int_fft && (L.tw64_nx != nx || L.tw64_ny != ny)) {
         WSG_CUDA(L.tw64x.ensure((size_t)2 * nx * sizeof(int4)));
         WSG_CUDA(L.tw64y.ensure((size_t)2 * ny * sizeof(int4)));

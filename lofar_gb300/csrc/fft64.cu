@@ -331,10 +331,10 @@ cudaError_t launch_dir(double2 *data, int nx, int ny, int planes, const int4 *tw
 
 }  // namespace
 
-bool fft64_supported(int nx, int ny)
+bool fft64_supported(int nx, int ny, long long planes)
 {
     auto ok = [](int n) { return n >= 256 && n <= 8192 && (n & (n - 1)) == 0; };
-    return ok(nx) && ok(ny);
+    return ok(nx) && ok(ny) && planes >= 1 && planes <= 65535;   // planes on grid.y
 }
 
 cudaError_t build_twiddles64(int4 *tw, int n, cudaStream_t stream)

@@ -231,9 +231,9 @@ struct FftMasks {
 bool fft_fused_supported(int nx, int ny, int tile);
 
 // FP64 per-plane 2D FFT on the integer pipe (fft64.cu): power-of-two edges
-// 256..8192; twiddles e^{+-2 pi i k / n} in Q62, 2n int4 entries per axis.
-// In place, unnormalised, times the exact power of two 2^post.
-bool fft64_supported(int nx, int ny);
+// 256..8192, up to 65535 planes; twiddles e^{+-2 pi i k / n} in Q62, 2n int4
+// entries per axis.  In place, unnormalised, times the exact power of two 2^post.
+bool fft64_supported(int nx, int ny, long long planes);
 cudaError_t build_twiddles64(int4 *tw, int n, cudaStream_t stream);
 cudaError_t launch_fft64(double2 *data, int nx, int ny, int planes, int sign,
                          const int4 *twx, const int4 *twy, int post, cudaStream_t stream);
