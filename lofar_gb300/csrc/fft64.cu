@@ -208,11 +208,21 @@ __global__ void __launch_bounds__(Fft64Shape<N>::THREADS, Fft64Shape<N>::MINB)
     // biased exponent of 2047 marks NaN and infinity).  Every thread runs
     // 4 IPT iterations.
     unsigned hi = 0u;
-    for (int f = tid; f < N * S::NTR; f += S::THREADS) {
+    constexpr int PER = N * S::NTR / S::THREADS;   // 4 IPT elements per thread
+    double2 ld[PER];
+#pragma unroll
+    for (int q = 0; q < PER; q++) {   // all loads in flight before the first use
         int tt, i;
         size_t g;
-        fft64_elem<N, COLS>(f, first, nx, tt, i, g);
-        const double2 v = base[g];
+        fft64_elem<N, COLS>(tid + q * S::THREADS, first, nx, tt, i, g);
+        ld[q] = base[g];
+    }
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        int tt, i;
+        size_t g;
+        fft64_elem<N, COLS>(tid + q * S::THREADS, first, nx, tt, i, g);
+        const double2 v = ld[q];
         sm64[tt * S::NP + i] = make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
         const unsigned h = max((unsigned)(__double_as_longlong(v.x) >> 32) & 0x7FFFFFFFu,
                                (unsigned)(__double_as_longlong(v.y) >> 32) & 0x7FFFFFFFu);
