@@ -311,13 +311,10 @@ cudaError_t launch_n(double2 *data, int nx, int ny, int planes, const int4 *tw, 
 {
     using S = Fft64Shape<N>;
     auto kern = k_fft64<N, SIGN, COLS>;
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(
-            kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // set on every launch: the attribute belongs to the current device
+    const cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    if (e != cudaSuccess) return e;
     const int count = COLS ? nx : ny;
     const dim3 grid(count / S::NTR, planes);
     kern<<<grid, S::THREADS, S::SMEM, stream>>>(data, nx, ny, SIGN > 0 ? tw : tw + N, post);
