@@ -985,6 +985,22 @@ def bench_driver(args, rank, world, peak, peak_kind):
     }
 
 
+NOMINAL_FP64_TFLOPS = 1.25   # GB300 dense FP64, nominal (no measured FP64 peak is recorded)
+
+
+def fft_fp64_equivalent(nx, planes, ms):
+    """FP64-equivalent rate of one direction's per-plane 2D FFTs, 5 N log2 N
+    flops per N-point plane, over `ms` (the FFT + w-correction stage: a lower
+    bound for the FFT alone)."""
+    npix = nx * nx
+    flop = 5.0 * npix * math.log2(npix) * planes
+    tf = flop / (ms * 1e-3) / 1e12
+    return {"tflops": tf, "of_nominal_fp64": tf / NOMINAL_FP64_TFLOPS,
+            "note": "5 N log2 N per plane over the FFT + w-correction stage time; the FFT "
+                    "runs in 64-bit fixed point on the integer pipe; nominal FP64 peak "
+                    f"{NOMINAL_FP64_TFLOPS} TFLOP/s"}
+
+
 def roofline(per, n, nx, P, sc, peak, peak_kind):
     ab = algorithmic_bytes(n, nx, nx, P, sc)
     med = {s: statistics.median(v) for s, v in per.items() if v}
@@ -1078,7 +1094,10 @@ def main():
                         # complex128 cube; the FP64 form runs its taps, FFT and
                         # w-correction in 64-bit fixed point, so its stages are
                         # bound by integer (and FP64 exponential) issue, not HBM
-                        "stages": roofline(f["per"], n, args.nx, args.planes, 16, peak, peak_kind)}
+                        "stages": roofline(f["per"], n, args.nx, args.planes, 16, peak, peak_kind),
+                        "fft_fp64_equivalent": fft_fp64_equivalent(
+                            args.nx, args.planes,
+                            statistics.median(f["per"]["fft_wcorrect"]))}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
     if not args.no_cpu and world >= 1:

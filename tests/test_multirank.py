@@ -78,3 +78,11 @@ def test_stage_roofline_arithmetic():
         assert st["degrid"]["frac"] == pytest.approx(ab["degrid"] / 2e-3 / 1e9 / 1000.0)
     assert bench.algorithmic_bytes(n, nx, nx, planes, 16)["fft_wcorrect"] == \
         2 * bench.algorithmic_bytes(n, nx, nx, planes, 8)["fft_wcorrect"]
+
+
+def test_fft_fp64_equivalent_rate():
+    import bench
+    r = bench.fft_fp64_equivalent(4096, 32, 25.0)
+    flop = 5.0 * 4096 * 4096 * 24 * 32
+    assert r["tflops"] == pytest.approx(flop / 25e-3 / 1e12)
+    assert r["of_nominal_fp64"] == pytest.approx(r["tflops"] / 1.25)
