@@ -171,7 +171,7 @@ def profiled_traffic(records):
         name = f[1].split("<")[0]
         if name in GRIDDING_KERNELS:
             try:
-                tot += (float(f[6]) + float(f[7])) * 1e9
+                tot += (float(f[5]) + float(f[6])) * 1e9
                 seen.add(name)
             except ValueError:
                 pass

@@ -116,8 +116,11 @@ typedef enum {
                        1e-11 (image) of the reference's FP64 arithmetic; the
                        taps, the FFT of power-of-two grids and the w-correction
                        run in 64-bit fixed point inside */
-    WSG_FP32C = 1   /* complex64 grid with compensated (two-float) tile
-                       accumulation; FP64-exact coordinates and phase argument */
+    WSG_FP32C = 1   /* complex64 grid; FP64-exact coordinates and phase
+                       argument.  Each tile is summed in int32 fixed point at
+                       a per-work-item scale (exact, order-independent sums;
+                       one rounding per tap); the partial tiles of a bin cut
+                       into several work items are combined with TwoSum */
 } wsg_precision;
 
 typedef struct wsg_plan wsg_plan;
@@ -318,7 +321,8 @@ WSG_API long long wsg_batch_device_bytes(wsg_batch *batch);
  *     (alignment included),
  *     nbins = num_w_planes*ceil(grid_size_y/64)*ceil(grid_size_x/64),
  * fails with WSG_ERR_CAPACITY (about 390,000 measurements on a 4096x4096x32
- * grid).  All calls share that array: calls whose GPU work may overlap race
+ * grid).  Each call overwrites the whole grid: a larger set is gridded part by
+ * part into separate grids that the caller sums.  All calls share that array: calls whose GPU work may overlap race
  * and must be serialised by the caller.  The first call on a device looks up
  * the array's device address and may load the device code: make it before
  * any stream capture.

@@ -1,6 +1,8 @@
 // C ABI of libwstack_gb300.so: the reference's drop-in entry points and the
 // device-resident plan API.  See include/wstack_gb300.h for the contract.
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <cufft.h>
 #include <math.h>
 #include <stdarg.h>
@@ -71,18 +73,29 @@ int wsg::report_status(int status, const char *msg)
     return set_error(status, "%s", msg ? msg : "");
 }
 
+// SM count of the current device, cached per device ordinal (a process may
+// drive GPUs with different SM counts from several threads).
 int wsg::num_sms()
 {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
-            v = 148;
-        n = v;
+    constexpr int kDevs = 64;
+    static std::atomic<int> cache[kDevs];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = 0;
     }
-    return n;
+    const bool cached = dev >= 0 && dev < kDevs;
+    if (cached) {
+        const int n = cache[dev].load(std::memory_order_relaxed);
+        if (n > 0) return n;
+    }
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        v = 148;
+    }
+    if (cached) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
 }
 
 // ---------------------------------------------------------------------------

@@ -16,8 +16,10 @@
 //     (alignment padding included),
 //     nbins = num_w_planes * ceil(grid_size_y/64) * ceil(grid_size_x/64),
 // and is rejected with WSG_ERR_CAPACITY when that exceeds the array: for a
-// 4096x4096x32 grid that is about 390,000 measurements per call.  Its bin
-// table keeps one counter per bin and kind (no sub-counters).
+// 4096x4096x32 grid that is about 390,000 measurements per call.  Every call
+// overwrites the whole grid (as wstack() does), so a caller splitting a larger
+// set grids each part into its own grid and sums the grids.  Its bin table
+// keeps one counter per bin and kind (no sub-counters).
 //
 // All calls share the array and it keeps what the last call left in it; each
 // call clears the counters it needs before using them.  Calls whose GPU work
@@ -150,6 +152,22 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     g.w_pow2 = pow2_recip(dw, k) ? 1 : 0;
     g.kw = g.w_pow2 ? k : 0;
 
+    // Bound the sizes before any layout arithmetic: a measurement needs at
+    // least 160 bytes of the array (four records of 40 bytes), so larger
+    // counts cannot fit and would overflow the products below; the value
+    // index m*freq_per_chan*polarizations must stay well inside 63 bits.
+    if ((unsigned long long)num_points > kNoAllocBytes / 160)
+        return fail(WSG_ERR_CAPACITY,
+                    "wsg_grid_noalloc: %ld measurements cannot fit its fixed %zu-byte scratch "
+                    "array (at most %zu); grid the parts into separate grids and sum them, or "
+                    "use the plan API",
+                    num_points, kNoAllocBytes, kNoAllocBytes / 160);
+    if (freq_per_chan > (1l << 20) || polarizations > (1l << 20) ||
+        (double)num_points * (double)freq_per_chan * (double)polarizations > 4.0e18)
+        return fail(WSG_ERR_ARG,
+                    "wsg_grid_noalloc: freq_per_chan %ld x polarizations %ld too large",
+                    freq_per_chan, polarizations);
+
     // scratch layout: counters | bin table | record cells | indices | fracs | values
     const unsigned long long cap = 4ull * (unsigned long long)(num_points > 0 ? num_points : 1);
     const size_t o_bins = up256(sizeof(DevCounters));
@@ -161,8 +179,9 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     if (g.nbins >= (1ll << 31) || need > kNoAllocBytes)
         return fail(WSG_ERR_CAPACITY,
                     "wsg_grid_noalloc: needs %zu bytes of scratch (about 32*%lld bins + 161*%ld "
-                    "measurements), above its fixed %zu-byte array; pass fewer measurements "
-                    "per call or use the plan API",
+                    "measurements), above its fixed %zu-byte array; every call overwrites the "
+                    "whole grid, so grid the parts into separate grids and sum them, or use "
+                    "the plan API",
                     need, g.nbins, num_points, kNoAllocBytes);
 
     void *base = nullptr;

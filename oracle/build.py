@@ -33,7 +33,23 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SO = os.path.join(REF_DIR, "libref.so")
 REFIO = os.path.join(REF_DIR, "refio")
-REFERENCE_TREE = os.environ.get("WSTACK_REFERENCE_TREE", "/root/reference")
+
+
+def _reference_tree() -> str:
+    """The reference checkout: ``--reference-tree DIR`` on the command line,
+    else ``WSTACK_REFERENCE_TREE``, else a ``reference/`` checkout beside this
+    repository.  Where none holds the sources, the reference builds are
+    skipped and the tests that pin the oracle to them skip too."""
+    for i, a in enumerate(sys.argv[:-1]):
+        if a == "--reference-tree":
+            return os.path.abspath(sys.argv[i + 1])
+    env = os.environ.get("WSTACK_REFERENCE_TREE")
+    if env:
+        return os.path.abspath(env)
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+REFERENCE_TREE = _reference_tree()
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"]
 

@@ -231,6 +231,24 @@ def image_adjoint(image_real, image_imag, uu, vv, ww, *, num_w_planes, dx, dw, w
 
 
 
+def grid_plane(w, uu, vv, ww, vis_real, vis_img, weight, *, num_w_planes, freq_per_chan=1,
+               polarizations=1, dx, dw, w_support, nx, ny, num_threads=0, out=None):
+    """Plane w of wstack(...) alone: [ny][nx][2] float64 (the reference's
+    gridding arithmetic, w-stacking.cu:243-306, restricted to the measurements
+    whose plane index is w), without the whole FP64 cube in memory."""
+    uu, vv, ww = _c(uu, np.float64), _c(vv, np.float64), _c(ww, np.float64)
+    vr, vi, wt = _c(vis_real, np.float32), _c(vis_img, np.float32), _c(weight, np.float32)
+    if out is None:
+        out = np.zeros((ny, nx, 2), np.float64)
+    else:
+        out[...] = 0.0
+    rows = np.zeros(ny, np.uint8)
+    load_oracle().oracle_grid_plane(w, num_w_planes, uu.shape[0], freq_per_chan, polarizations,
+                                    _dp(uu), _dp(vv), _dp(ww), _fp(vr), _fp(vi), _fp(wt), dx, dw,
+                                    w_support, nx, ny, _dp(out), rows.ctypes.data, num_threads)
+    return out
+
+
 def _ifft_rows(g, workers):
     try:
         import scipy.fft as sfft

@@ -80,3 +80,47 @@ def test_noalloc_refuses_what_it_cannot_hold(gpu):
                               h.ctypes.data, h.ctypes.data, h.ctypes.data, 1 / 64, 0.25, 7, 64, 64,
                               grid.data_ptr(), None)
     assert st == _lib.WSG_ERR_ARG
+
+
+def test_noalloc_folds_channels_and_polarisations_at_the_grid_edges(gpu):
+    """freq_per_chan = polarizations = 2 with NaN-flagged entries, and
+    measurements just inside u = 0, v = 0 and the far grid edges, whose
+    support windows are clipped: the no-allocation binning and scatter run
+    with their own parameters (no sub-counters, no partial tiles), so they are
+    checked here against wstack() at 1e-12."""
+    import torch
+
+    import lofar_gb300 as L
+    from lofar_gb300 import _lib
+
+    lib = _lib.load()
+    L.set_precision("fp64")
+    rng = np.random.default_rng(31)
+    nx, ny, planes, support, nf, npol = 96, 80, 4, 7, 2, 2
+    n = 20_000
+    uu = rng.random(n)
+    vv = rng.random(n)
+    edge = rng.choice(n, 4000, replace=False)
+    side = rng.integers(0, 4, edge.size)
+    eps = rng.random(edge.size) * 2.5 / nx
+    uu[edge[side == 0]] = eps[side == 0]                          # just inside u = 0
+    vv[edge[side == 1]] = eps[side == 1]                          # just inside v = 0
+    uu[edge[side == 2]] = np.minimum(1.0 - eps[side == 2], np.nextafter(1.0, 0.0))
+    vv[edge[side == 3]] = np.minimum(1.0 - eps[side == 3], np.nextafter(1.0, 0.0))
+    ww = rng.random(n) * 0.999
+    vr = rng.standard_normal(n * nf * npol).astype(np.float32)
+    vi = rng.standard_normal(n * nf * npol).astype(np.float32)
+    vr[rng.choice(vr.size, 500, replace=False)] = np.nan           # flagged: skipped
+    wt = rng.random(n * npol).astype(np.float32)
+    ref = np.zeros((planes, ny, nx, 2))
+    L.wstack(planes, n, nf, npol, uu, vv, ww, vr, vi, wt, 1.0 / nx, 1.0 / planes, support, nx,
+             ny, ref, 1)
+    dev = [torch.as_tensor(a).cuda() for a in (uu, vv, ww, vr, vi, wt)]
+    grid = torch.full((planes, ny, nx, 2), -1.0, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(2):
+        st = lib.wsg_grid_noalloc(planes, n, nf, npol, *(t.data_ptr() for t in dev), 1.0 / nx,
+                                  1.0 / planes, support, nx, ny, grid.data_ptr(), None)
+        assert st == _lib.WSG_OK, _lib.last_error()
+        torch.cuda.synchronize()
+        assert _nrm_max(grid.cpu().numpy(), ref) <= 1e-12
