@@ -264,7 +264,7 @@ def run_plan_steps(plan, ins, image, out, steps, record_stages):
         plan.bin(*ins)
         if evs:
             evs[1].record(stream)
-        grid = plan.grid(plan_grid(plan))
+        grid = plan.grid(plan_grid(plan), occupied_only=True)
         if evs:
             evs[2].record(stream)
         plan.fft_wcorrect(grid, out=image)

@@ -166,6 +166,11 @@ WSG_API int wsg_bin(wsg_plan *plan, long num_points, long freq_per_chan, long po
             const float *vis_img, const float *weight);
 /* Grid the binned measurements; grid is overwritten (every cell written). */
 WSG_API int wsg_grid(wsg_plan *plan, void *grid);
+/* As wsg_grid, but only the tiles that hold measurements are written; the
+ * other tiles of `grid` keep their contents.  Those tiles are exactly the ones
+ * wsg_fft_wcorrect reads with pruning on a fused FP32C plan, so this pair is
+ * the staged form of wsg_image_forward.  On other plans it equals wsg_grid. */
+WSG_API int wsg_grid_occupied(wsg_plan *plan, void *grid);
 /* Unnormalised per-plane 2D FFT in place; sign +1 = exponent +i
  * (FFTW_BACKWARD, the forward imaging direction), -1 = exponent -i. */
 WSG_API int wsg_fft(wsg_plan *plan, void *grid, int sign);
@@ -230,7 +235,9 @@ WSG_API int wsg_image_forward_host_async(wsg_plan *plan, long num_points, long f
 WSG_API int wsg_image_adjoint_host_async(wsg_plan *plan, const void *image, void *out);
 WSG_API int wsg_plan_synchronize(wsg_plan *plan);
 
-/* Resident grid of the plan ([P][Ny][Nx] complex), for inspection. */
+/* Resident cube buffer of the plan ([P][Ny][Nx] complex): the grid after
+ * wsg_grid; wsg_image_forward uses it as its work buffer (on fused FP32C plans
+ * the tiles without measurements are left unwritten there). */
 WSG_API void *wsg_plan_grid(wsg_plan *plan);
 
 /* Times candidate settings of the tile edge, split size and persistent CTA
@@ -301,7 +308,8 @@ WSG_API int wsg_batch_autotune(wsg_batch *batch, void *images, int iters, wsg_tu
 /* First visibility of `channel` in vis_out; channel = num_channels gives the
  * total (-1 before wsg_batch_bind). */
 WSG_API long long wsg_batch_vis_offset(wsg_batch *batch, int channel);
-/* Resident grids of the last forward ([channel][pol][P][Ny][Nx] complex64). */
+/* Resident cube buffer of the batch ([channel][pol][P][Ny][Nx] complex64): the
+ * forward's work buffer (column-transformed planes of the occupied tiles). */
 WSG_API void *wsg_batch_grids(wsg_batch *batch);
 WSG_API int wsg_batch_get_stats(wsg_batch *batch, wsg_stats *stats);
 WSG_API long long wsg_batch_device_bytes(wsg_batch *batch);

@@ -123,6 +123,7 @@ SIGNATURES = {
     "wsg_plan_grid": (_P, [_P]),
     "wsg_bin": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P]),
     "wsg_grid": (_I, [_P, _P]),
+    "wsg_grid_occupied": (_I, [_P, _P]),
     "wsg_fft": (_I, [_P, _P, _I]),
     "wsg_wcorrect": (_I, [_P, _P, _P, _D]),
     "wsg_wcorrect_adjoint": (_I, [_P, _P, _P, _D]),

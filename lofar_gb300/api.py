@@ -180,11 +180,14 @@ class Plan:
     def new_grid(self):
         return self._torch.empty((self.planes, self.ny, self.nx), dtype=self.cdtype, device="cuda")
 
-    def grid(self, out=None):
+    def grid(self, out=None, occupied_only: bool = False):
+        """Grid the binned measurements.  occupied_only: write only the tiles
+        that hold measurements (the input fft_wcorrect reads with pruning)."""
         out = self.new_grid() if out is None else out
         assert out.dtype == self.cdtype and out.is_contiguous() and out.numel() == self.planes * self.ny * self.nx
         self._sync_stream()
-        check(self.lib.wsg_grid(self._h, out.data_ptr()))
+        fn = self.lib.wsg_grid_occupied if occupied_only else self.lib.wsg_grid
+        check(fn(self._h, out.data_ptr()))
         return out
 
     def fft(self, grid, sign: int = +1):

@@ -77,7 +77,7 @@ int batch_enqueue_forward(wsg_batch *B, void *images)
     WSG_CUDA(launch_bin_scatter_batch(p->geom, p->prec, B->tab, b, r, p->stream));
     WSG_CUDA(launch_fft_masks(p->geom, b, mask_view(p), p->stream));
     WSG_CUDA(launch_grid(p->geom, p->prec, b, r, p->grid.p, p->partials.p, p->ctas_grid,
-                         p->stream));
+                         p->stream, true));   // occupied tiles only: the fused transforms skip the rest
     WSG_CUDA(launch_image_fwd_fused(p->geom, p->grid.as<float2>(), reinterpret_cast<float2 *>(images),
                                     p->twx.as<float2>(), p->twy.as<float2>(), plan_wscreen(p),
                                     mask_view(p), p->wc.phase_on && p->planes > 1,

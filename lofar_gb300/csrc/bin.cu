@@ -75,9 +75,18 @@ __device__ __forceinline__ unsigned bin_index(const GeomParams &g, int w, int tv
 // operations in flight per thread.
 constexpr int kItems = 4;
 
-__device__ __forceinline__ unsigned sub_of(long long m, unsigned nsub)
+// Sub-range of a record within its bin: the 4x4 block (T/4 cells square) of
+// its tile-relative cell, clamped to the tile, in Morton order; one range
+// when nsub < 16.  The tile kernels then meet a bin's records block by block,
+// so each of their sorted stages covers a compact area.
+__device__ __forceinline__ unsigned sub_key(const GeomParams &g, unsigned nsub, int cell_u,
+                                            int cell_v, int tu, int tv)
 {
-    return (unsigned)(m >> 8) & (nsub - 1u);
+    if (nsub < 16u) return 0u;
+    const int t1 = g.tile - 1;
+    const unsigned bx = (unsigned)min(max(cell_u - (tu << g.tile_shift), 0), t1) >> (g.tile_shift - 2);
+    const unsigned by = (unsigned)min(max(cell_v - (tv << g.tile_shift), 0), t1) >> (g.tile_shift - 2);
+    return (bx & 1u) | ((by & 1u) << 1) | ((bx & 2u) << 1) | ((by & 2u) << 2);
 }
 
 template <bool UP2, bool WP2>
@@ -106,17 +115,18 @@ k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restric
             const int st = m < n ? measure<UP2, WP2, float>(g, x[i], y[i], z[i], o, fu, fv) : 3;
             ndp += st == 1;
             ndw += st == 2;
-            const unsigned sub = sub_of(m, b.nsub);
-            const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
+            // primaries: one aggregated atomic per (sub-range, bin) and warp
+            const unsigned prim = (st == 0) ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) * nb +
+                                                  bin_index(g, o.gw, o.tvp, o.tup)
+                                            : kFull;
             const unsigned peers = __match_any_sync(kFull, prim);
             if (st == 0) {
-                // lanes of one warp share m >> 8, hence the sub-counter
-                if (lane == __ffs(peers) - 1)
-                    atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
+                if (lane == __ffs(peers) - 1) atomicAdd(&b.sub_prim[prim], (unsigned)__popc(peers));
                 for (int tv = o.tv0; tv <= o.tv1; tv++)
                     for (int tu = o.tu0; tu <= o.tu1; tu++)
                         if (tv != o.tvp || tu != o.tup)
-                            atomicAdd(&b.sub_dup[sub * nb + bin_index(g, o.gw, tv, tu)], 1u);
+                            atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb +
+                                                 bin_index(g, o.gw, tv, tu)], 1u);
             }
         }
         for (int d = 16; d >= 1; d >>= 1) {
@@ -202,12 +212,13 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             MGeom o;
             S fu, fv;
             const int st = m < n ? measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv) : 3;
-            const unsigned prim = (st == 0) ? bin_index(g, o.gw, o.tvp, o.tup) : kFull;
+            const unsigned prim = (st == 0) ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) * nb +
+                                                  bin_index(g, o.gw, o.tvp, o.tup)
+                                            : kFull;
             const unsigned peers = __match_any_sync(kFull, prim);
             const int leader = __ffs(peers) - 1;
             unsigned got = 0;
-            if (st == 0 && lane == leader)
-                got = atomicAdd(&b.sub_prim[sub_of(m, b.nsub) * nb + prim], (unsigned)__popc(peers));
+            if (st == 0 && lane == leader) got = atomicAdd(&b.sub_prim[prim], (unsigned)__popc(peers));
             const unsigned basep = __shfl_sync(kFull, got, leader);
             ppos[i] = (st == 0) ? basep + (unsigned)__popc(peers & lt_mask) : 0xFFFFFFFFu;
         }
@@ -229,9 +240,10 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             for (int tv = o.tv0; tv <= o.tv1; tv++) {
                 for (int tu = o.tu0; tu <= o.tu1; tu++) {
                     const unsigned bin = bin_index(g, o.gw, tv, tu);
-                    const unsigned pos = (tv == o.tvp && tu == o.tup)
-                                             ? ppos[i]
-                                             : atomicAdd(&b.sub_dup[sub_of(m, b.nsub) * nb + bin], 1u);
+                    const unsigned pos =
+                        (tv == o.tvp && tu == o.tup)
+                            ? ppos[i]
+                            : atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb + bin], 1u);
                     const int cu = o.gu - (tu << g.tile_shift);
                     const int cv = o.gv - (tv << g.tile_shift);
                     if (PREC == WSG_FP64) {
@@ -315,18 +327,18 @@ __global__ void __launch_bounds__(256) k_bin_count_batch(GeomParams g, ChanTable
         float fu, fv;
         BatchPoint bp;
         const int st = batch_point<UP2, WP2, float>(g, t, s_m0, m, o, fu, fv, bp);
-        const unsigned sub = sub_of(m, b.nsub);
+        const unsigned psub = st == 0 ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) : 0u;
         for (int p = 0; p < t.pols; p++) {
             const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
-            const unsigned prim = (st == 0) ? bin_index(g, plane, o.tvp, o.tup) : kFull;
+            const unsigned prim = (st == 0) ? psub * nb + bin_index(g, plane, o.tvp, o.tup) : kFull;
             const unsigned peers = __match_any_sync(kFull, prim);
             if (st == 0) {
-                if (lane == __ffs(peers) - 1)
-                    atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
+                if (lane == __ffs(peers) - 1) atomicAdd(&b.sub_prim[prim], (unsigned)__popc(peers));
                 for (int tv = o.tv0; tv <= o.tv1; tv++)
                     for (int tu = o.tu0; tu <= o.tu1; tu++)
                         if (tv != o.tvp || tu != o.tup)
-                            atomicAdd(&b.sub_dup[sub * nb + bin_index(g, plane, tv, tu)], 1u);
+                            atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb +
+                                                 bin_index(g, plane, tv, tu)], 1u);
             }
         }
         int ndp = st == 1, ndw = st == 2;
@@ -359,15 +371,14 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
         S fu, fv;
         BatchPoint bp;
         const int st = batch_point<UP2, WP2, S>(g, t, s_m0, m, o, fu, fv, bp);
-        const unsigned sub = sub_of(m, b.nsub);
+        const unsigned psub = st == 0 ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) : 0u;
         for (int p = 0; p < t.pols; p++) {
             const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
-            const unsigned prim = (st == 0) ? bin_index(g, plane, o.tvp, o.tup) : kFull;
+            const unsigned prim = (st == 0) ? psub * nb + bin_index(g, plane, o.tvp, o.tup) : kFull;
             const unsigned peers = __match_any_sync(kFull, prim);
             const int leader = __ffs(peers) - 1;
             unsigned got = 0;
-            if (st == 0 && lane == leader)
-                got = atomicAdd(&b.sub_prim[sub * nb + prim], (unsigned)__popc(peers));
+            if (st == 0 && lane == leader) got = atomicAdd(&b.sub_prim[prim], (unsigned)__popc(peers));
             const unsigned basep = __shfl_sync(kFull, got, leader);
             if (st != 0) continue;
             const unsigned ppos = basep + (unsigned)__popc(peers & lt_mask);
@@ -384,7 +395,9 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
                 for (int tu = o.tu0; tu <= o.tu1; tu++) {
                     const bool primary = tv == o.tvp && tu == o.tup;
                     const unsigned pos =
-                        primary ? ppos : atomicAdd(&b.sub_dup[sub * nb + bin_index(g, plane, tv, tu)], 1u);
+                        primary ? ppos
+                                : atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb +
+                                                       bin_index(g, plane, tv, tu)], 1u);
                     const int cu = o.gu - (tu << g.tile_shift);
                     const int cv = o.gv - (tv << g.tile_shift);
                     if (PREC == WSG_FP64) {
@@ -589,6 +602,7 @@ __global__ void __launch_bounds__(kScanThreads) k_bin_scan_c(long long nbins, Bi
         b.ntotal[i] = t;
         b.off[i] = (unsigned)r0;
         b.is_split[i] = it ? 1u : 0u;
+        if (t && !it) b.work[atomicAdd(&b.ctr->nwork, 1u)] = (unsigned)i;
         b.slot[i] = (unsigned)(r1 >> 32);
         b.done[i] = 0u;
         const unsigned first = (unsigned)(r1 & 0xFFFFFFFFull);

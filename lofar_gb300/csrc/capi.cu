@@ -138,7 +138,7 @@ int wsg::plan_configure(wsg_plan *p)
     g.ku = g.u_pow2 ? k : 0;
     g.w_pow2 = is_pow2_recip(p->dw, k) ? 1 : 0;
     g.kw = g.w_pow2 ? k : 0;
-    if (g.nbins >= (1ll << 32) - 1)
+    if (g.nbins * kSub >= (1ll << 32) - 1)
         return set_error(WSG_ERR_UNSUPPORTED, "too many (plane, tile) bins: %lld", g.nbins);
     const int sms = num_sms();
     const int og = grid_max_ctas_per_sm(p->prec, p->tile, p->half);
@@ -302,6 +302,9 @@ int wsg_plan_create(wsg_plan **out, int grid_size_x, int grid_size_y, int num_w_
     p->dw = dw;
     p->stream = (cudaStream_t)stream;
     p->tile = 64;
+    // FP32C work items sort and sum up to 16384 records in stages; the FP64
+    // gridder sums items of up to 4096 records in fixed point
+    p->split = precision == WSG_FP32C ? kDefaultSplitF32 : kDefaultSplit;
     int st = WSG_OK;
     cudaError_t e = p->ctr.ensure(sizeof(DevCounters));
     if (e != cudaSuccess) st = set_error(WSG_ERR_NOMEM, "%s", cudaGetErrorString(e));
@@ -474,6 +477,18 @@ int wsg_grid(wsg_plan *p, void *grid)
     return WSG_OK;
 }
 
+int wsg_grid_occupied(wsg_plan *p, void *grid)
+{
+    clear_error();
+    if (!p || !grid) return set_error(WSG_ERR_ARG, "NULL argument");
+    if (p->n_binned < 0) return set_error(WSG_ERR_STATE, "wsg_grid_occupied before wsg_bin");
+    const BinBuffers b = p->binbufs();
+    WSG_CUDA(cudaMemsetAsync(&b.ctr->work_grid, 0, sizeof(unsigned), p->stream));
+    WSG_CUDA(launch_grid(p->geom, p->prec, b, p->recbufs(), grid, p->partials.p, p->ctas_grid,
+                         p->stream, p->fused));
+    return WSG_OK;
+}
+
 int wsg_fft(wsg_plan *p, void *grid, int sign)
 {
     clear_error();
@@ -618,7 +633,9 @@ int wsg_image_forward(wsg_plan *p, long n, long nf, long np, const double *uu, c
     WSG_CUDA(p->grid.ensure(p->elem() * (size_t)p->cube_planes() * p->npix()));
     WSG_TRY(ensure_wscreen(p));
     WSG_TRY(wsg_bin(p, n, nf, np, uu, vv, ww, vr, vi, wt));
-    WSG_TRY(wsg_grid(p, p->grid.p));
+    // the fused transforms read occupied tiles only: the gridder skips the
+    // tiles of empty bins, which would only be written with zeros
+    WSG_TRY(wsg_grid_occupied(p, p->grid.p));
     WSG_TRY(wsg_fft_wcorrect(p, p->grid.p, image, 1));
     return WSG_OK;
 }

@@ -43,6 +43,7 @@ struct GridArgs {
     RecBuffers r;
     void *grid;
     void *partials;
+    int sparse;   // FP32C: occupied bins only (the list b.work)
 };
 
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
@@ -84,46 +85,97 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
     return b.is_split[bin] == 0u;
 }
 
-// FP32C tile kernel.  A warp pass takes RPW = 32/NT records; lane (g, k) of
-// record g owns row k of its support window: it evaluates the column weight
-// gu_k and the row weight gv_k of the separable Gaussian once, then walks the
-// NT columns of its row, fetching gu_j from lane (g, j) with a shuffle and
-// adding V*gv_k*gu_j into the shared-memory accumulator (odd pitch: the NT
-// rows of one record fall in distinct banks).  Records are staged into shared
-// memory kStage at a time with coalesced 16-byte loads.
+// FP32C tile kernel: records sorted by cell in shared memory, taps of
+// consecutive records of one cell summed in registers, one shared-memory
+// atomic per cell and run of records instead of one per tap (the run-length
+// idea of Romein, "An efficient work-distribution strategy for gridding
+// radio-telescope data on GPUs", ICS 2012, applied to sorted runs).
 //
-// The accumulator is int32 fixed point: shared-memory integer atomics retire
-// about five times faster than float ones on this part.  Each work item first
-// bounds its largest cell from the local sums of |Re V| + |Im V| (see below)
-// and picks the scale 2^f that keeps every cell sum below 2^30, with room for
-// the rounding of each term.  The integer sums are exact and
-// order-independent; the only error is the rounding of each tap to the
-// item's quantum, 2^-f.
+// An item is processed in stages of at most kStageR records.  A stage is
+// loaded into shared memory with coalesced 16-byte loads and counting-sorted
+// by the Morton index of its (clamped) tile-relative cell, so the records of
+// one cell are consecutive: at 4096^2 x 32 planes and 50M measurements a
+// populated cell holds ~14 records, and the binning orders each bin's records
+// by blocks of T/4 x T/4 cells, so a stage covers a compact area at the bin's
+// own density.  The sorted stage is cut into NS contiguous streams, one per
+// group of NT = 2K+1 lanes (RPW groups per warp).
 //
-// The accumulator has a 2K halo on every side so that every tap of every
-// record of the bin lands in it without a bounds test; the halo is never read
-// and is not cleared (it only collects the taps of neighbouring tiles).
-template <int T, int K>
-__global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
+// Lane k of a group owns window row k of its stream's records and keeps NT
+// register accumulators, one per window column.  While consecutive records
+// sit in the same cell their windows cover the same cells, so the taps keep
+// summing in registers; when the cell changes, and at the end of the stream,
+// the accumulators are added to the shared-memory tile (integer atomics at an
+// odd pitch, so the NT rows of a window fall in distinct banks; cells outside
+// the tile, which only duplicates of neighbouring tiles reach, are skipped).
+//
+// Tap arithmetic is that of the separable Gaussian: lane k evaluates the row
+// weight gv of row k and the column weight gu of column k; the other column
+// weights come by shuffles.  Each tap V*gv*gu is rounded to the item's
+// fixed-point quantum with one FMA against 1.5*2^23 and summed as an int32, so
+// sums are exact and independent of order: an unsplit bin grids to the same
+// bits whatever the order of its records and wherever the runs break.  The
+// scale 2^f of an item keeps every cell sum below 2^30 (see the bound below;
+// a partial sum of a cell is bounded by the same sum of absolute values) and
+// every tap below 2^22.
+
+// Threads per CTA of the FP32C gridder: 512 (two CTAs per SM, 64 registers a
+// thread) up to support 7; 256 for wider supports, whose 2*(2K+1) register
+// accumulators per lane need more registers.
+constexpr int f32c_threads(int half) { return half >= 4 ? 256 : 512; }
+constexpr int kStageR = 2048;    // records per sorted stage (16-bit indices)
+
+__device__ __forceinline__ unsigned spread6(unsigned x)
 {
+    x = (x | (x << 4)) & 0x0F0Fu;
+    x = (x | (x << 2)) & 0x3333u;
+    x = (x | (x << 1)) & 0x5555u;
+    return x;
+}
+
+// Bytes of the two int32 accumulator tiles (pitch T + 1), 16-byte aligned.
+template <int T> constexpr size_t acc_bytes() { return ((size_t)8 * T * (T + 1) + 15) / 16 * 16; }
+
+// Sort key of a record: Morton index of its cell clamped to the tile.
+template <int T>
+__device__ __forceinline__ unsigned cell_key(const uint4 &q)
+{
+    const int cu = min(max((int)(q.x >> 24) - 64, 0), T - 1);
+    const int cv = min(max((int)(q.y >> 24) - 64, 0), T - 1);
+    return spread6((unsigned)cu) | (spread6((unsigned)cv) << 1);
+}
+
+template <int T, int K>
+__global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
+{
+    constexpr int kThreadsR = f32c_threads(K);
     constexpr int NT = 2 * K + 1;
     constexpr int RPW = 32 / NT;
+    constexpr int NW = kThreadsR / 32;
+    constexpr int NS = NW * RPW;                 // record streams per stage
     constexpr int H = 2 * K;
-    constexpr int AW = T + 2 * H;
-    constexpr int AP = AW | 1;
-    constexpr int NW = kThreads / 32;
-    constexpr int CPT = T * T / kThreads;
-    constexpr int ACC = ((2 * AW * AP * 4) + 15) / 16 * 16;
+    constexpr int AW = T + 2 * H;                // area of the bound's blocks
+    constexpr int BS = K <= 4 ? 2 : 3;           // bound blocks of 2^BS cells, >= K
+    constexpr int NB = (AW + (1 << BS) - 1) >> BS;   // blocks per side
+    constexpr int NKEY = T * T;                  // sort buckets
+    constexpr int KW = NKEY / 2 / kThreadsR;     // packed bucket words per thread
+    constexpr int RPT = kStageR / kThreadsR;     // staged records per thread
+    constexpr int CPT = T * T / kThreadsR;
+    constexpr int TP = T + 1;                    // accumulator pitch (odd)
+    constexpr int kNoCell = -(1 << 20);
+    static_assert(KW >= 1 && NKEY / 2 == KW * kThreadsR, "bucket words per thread");
+    static_assert(kStageR < 65536, "16-bit record indices and bucket counts");
     extern __shared__ __align__(16) unsigned char smraw[];
     int *are = reinterpret_cast<int *>(smraw);
-    int *aim = are + AW * AP;
-    uint4 *stage = reinterpret_cast<uint4 *>(smraw + ACC);
-    __shared__ unsigned s_item;
+    int *aim = are + T * TP;
+    uint4 *stage = reinterpret_cast<uint4 *>(smraw + acc_bytes<T>());
+    unsigned *hist = reinterpret_cast<unsigned *>(stage + kStageR);   // 2 counts per word
+    unsigned short *sidx = reinterpret_cast<unsigned short *>(hist + NKEY / 2);
+    __shared__ unsigned s_item[2];
     __shared__ int s_last;
-    constexpr int NB = (AW + 7) / 8;   // 8x8-cell blocks of the accumulator
     __shared__ float s_part[NW];
     __shared__ float s_vmax[NW];
     __shared__ unsigned s_blk[NB * NB];
+    __shared__ unsigned s_wsum[NW];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int grp = lane / NT, k = lane - (lane / NT) * NT;
@@ -135,19 +187,28 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
     float2 *grid = reinterpret_cast<float2 *>(a.grid);
     float2 *parts = reinterpret_cast<float2 *>(a.partials);
     const unsigned nsplit = a.b.ctr->nsplit_items;
-    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+    const unsigned nitems = nsplit + (a.sparse ? a.b.ctr->nwork : (unsigned)a.g.nbins);
     const unsigned split = a.b.split_size;
 
-    for (int i = tid; i < 2 * AW * AP; i += kThreads) are[i] = 0;
+    for (int i = tid; i < 2 * T * TP; i += kThreadsR) are[i] = 0;
+    // work items come from a global counter; the next one is fetched while
+    // the current one is processed, which hides the atomic's latency
+    if (tid == 0) s_item[0] = atomicAdd(&a.b.ctr->work_grid, 1u);
+    int slot = 0;
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) s_item = atomicAdd(&a.b.ctr->work_grid, 1u);
-        __syncthreads();
-        const unsigned item = s_item;
+        const unsigned item = s_item[slot];
         if (item >= nitems) break;
+        if (tid == 0) s_item[slot ^ 1] = atomicAdd(&a.b.ctr->work_grid, 1u);
+        slot ^= 1;
         unsigned bin, chunk;
-        if (!work_item(a.b, item, nsplit, bin, chunk)) continue;
+        if (a.sparse && item >= nsplit) {
+            bin = a.b.work[item - nsplit];
+            chunk = 0;
+        } else if (!work_item(a.b, item, nsplit, bin, chunk)) {
+            continue;
+        }
         int w, u0, v0;
         decode_bin(a.g, bin, w, u0, v0);
         const int tx = min(T, a.g.nx - u0);
@@ -158,18 +219,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         const unsigned r1 = is_split ? min(total, r0 + split) : total;
         const unsigned off = a.b.off[bin];
 
-        // The item's scale.  Sum |Re V| + |Im V| of the records per 8x8 block
-        // of the accumulator (by centre cell); a cell's taps all come from
-        // records centred within K <= 7 cells, i.e. in its block or the 8
+        // The item's scale.  Sum |Re V| + |Im V| of the records per block of
+        // 2^BS x 2^BS cells (2^BS >= K) of the area the records are centred in
+        // (records of neighbouring tiles' halos included); a cell's taps all
+        // come from records centred within K cells, i.e. in its block or the 8
         // around it, so the largest 3x3-block sum times the peak weight norm
-        // bounds every cell of the item.  The block sums are integers: each
-        // term is rounded up at a scale taken from the item's largest value
-        // and record count (sums stay below 2^31), so the bound is an upper
-        // bound, independent of the order of the records, and costs integer
-        // shared-memory atomics instead of float ones.
-        for (int i = tid; i < NB * NB; i += kThreads) s_blk[i] = 0u;
+        // bounds every cell of the item, and every partial sum of a cell.  The
+        // block sums are integers: each term is rounded up at a scale taken
+        // from the item's largest value and record count (sums stay below
+        // 2^31), so the bound is an upper bound, independent of the order of
+        // the records.
+        for (int i = tid; i < NB * NB; i += kThreadsR) s_blk[i] = 0u;
         float vmax = 0.0f;
-        for (unsigned i = r0 + tid; i < r1; i += kThreads) {
+        for (unsigned i = r0 + tid; i < r1; i += kThreadsR) {
             const uint4 q = __ldcg(rec + off + i);
             vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(q.z)), fabsf(__uint_as_float(q.w))));
         }
@@ -186,17 +248,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
             const int lb = 32 - __clz(r1 - r0);     // record count < 2^lb
             const int sc = min(30 - lb - ev, 126);  // terms <= 2^(31-lb): sums < 2^31
             const float up = ldexpf(1.0f, sc);
-            for (unsigned i = r0 + tid; i < r1; i += kThreads) {
+            for (unsigned i = r0 + tid; i < r1; i += kThreadsR) {
                 const uint4 q = __ldcg(rec + off + i);
-                const int bx = ((int)(q.x >> 24) - 64 + H) >> 3;
-                const int by = ((int)(q.y >> 24) - 64 + H) >> 3;
+                const int bx = ((int)(q.x >> 24) - 64 + H) >> BS;
+                const int by = ((int)(q.y >> 24) - 64 + H) >> BS;
                 const float v = fabsf(__uint_as_float(q.z)) + fabsf(__uint_as_float(q.w));
                 // v*up rounded up twice: the product toward +inf, then ceil
                 atomicAdd(&s_blk[by * NB + bx], (unsigned)ceilf(__fmul_ru(v, up)));
             }
             __syncthreads();
             unsigned long long bmax = 0ull;
-            for (int i = tid; i < NB * NB; i += kThreads) {
+            for (int i = tid; i < NB * NB; i += kThreadsR) {
                 const int by = i / NB, bx = i - (i / NB) * NB;
                 unsigned long long t = 0ull;
                 for (int yy = max(by - 1, 0); yy <= min(by + 1, NB - 1); yy++)
@@ -225,15 +287,79 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         const float scale = ldexpf(1.0f, fexp);
         const float inv = ldexpf(1.0f, -fexp);
 
-        for (unsigned c0 = r0; c0 < r1; c0 += kStage) {
-            const unsigned cnt = min((unsigned)kStage, r1 - c0);
+        const unsigned n = r1 - r0;
+        const unsigned nst = (n + kStageR - 1) / kStageR;
+        const unsigned per = nst ? (n + nst - 1) / nst : 0u;
+        for (unsigned st = 0; st < nst; st++) {
+            const unsigned c0 = r0 + st * per;
+            const unsigned cnt = min(per, r1 - c0);
+            __syncthreads();   // the previous stage's streams are done with stage/sidx
+            for (int i = tid; i < NKEY / 2; i += kThreadsR) hist[i] = 0u;
+            unsigned key[RPT];
+#pragma unroll
+            for (int t = 0; t < RPT; t++) {
+                const unsigned i = tid + t * kThreadsR;
+                key[t] = 0u;
+                if (i < cnt) {
+                    const uint4 q = __ldcs(rec + off + c0 + i);
+                    stage[i] = q;
+                    key[t] = cell_key<T>(q);
+                }
+            }
             __syncthreads();
-            for (unsigned i = tid; i < cnt; i += kThreads) stage[i] = __ldcs(rec + off + c0 + i);
+#pragma unroll
+            for (int t = 0; t < RPT; t++)
+                if (tid + t * kThreadsR < cnt)
+                    atomicAdd(&hist[key[t] >> 1], (key[t] & 1u) ? 0x10000u : 1u);
             __syncthreads();
-            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
-                const unsigned r = base + grp;
-                const bool valid = lane_on && r < cnt;
-                const uint4 q = stage[valid ? r : 0];
+            // exclusive scan of the bucket counts (two 16-bit counts per word,
+            // buckets in key order); a cursor never exceeds cnt < 2^16
+            {
+                unsigned wv[KW];
+                unsigned run = 0u;
+#pragma unroll
+                for (int t = 0; t < KW; t++) {
+                    wv[t] = hist[tid * KW + t];
+                    run += (wv[t] & 0xFFFFu) + (wv[t] >> 16);
+                }
+                unsigned incl = run;
+                for (int d = 1; d < 32; d <<= 1) {
+                    const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+                    if (lane >= d) incl += y;
+                }
+                if (lane == 31) s_wsum[warp] = incl;
+                __syncthreads();
+                unsigned base = incl - run;
+                for (int i = 0; i < warp; i++) base += s_wsum[i];
+#pragma unroll
+                for (int t = 0; t < KW; t++) {
+                    const unsigned lo = wv[t] & 0xFFFFu, hi = wv[t] >> 16;
+                    hist[tid * KW + t] = base | ((base + lo) << 16);
+                    base += lo + hi;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int t = 0; t < RPT; t++) {
+                const unsigned i = tid + t * kThreadsR;
+                if (i < cnt) {
+                    const unsigned old = atomicAdd(&hist[key[t] >> 1], (key[t] & 1u) ? 0x10000u : 1u);
+                    sidx[(key[t] & 1u) ? (old >> 16) : (old & 0xFFFFu)] = (unsigned short)i;
+                }
+            }
+            __syncthreads();
+
+            // the streams
+            const unsigned len = (cnt + NS - 1) / NS;
+            const unsigned sbeg = (unsigned)(warp * RPW + grp) * len;
+            int acc_r[NT], acc_i[NT];
+#pragma unroll
+            for (int j = 0; j < NT; j++) acc_r[j] = acc_i[j] = 0;
+            int pcu = kNoCell, pcv = kNoCell;   // cell of the run being summed
+            for (unsigned t = 0; t < len; t++) {
+                const unsigned ri = sbeg + t;
+                const bool valid = lane_on && ri < cnt;
+                const uint4 q = stage[sidx[valid ? ri : 0u]];
                 const int cu = (int)(q.x >> 24) - 64;
                 const int cv = (int)(q.y >> 24) - 64;
                 const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
@@ -241,37 +367,65 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
                 const float du = off1 - fu, dv = off1 - fv;
                 const float gu = norm * fast_exp2(du * du * c2);
                 const float gv = fast_exp2(dv * dv * c2) * scale;
-                const float ar = __uint_as_float(q.z) * gv;
-                const float ai = __uint_as_float(q.w) * gv;
-                const int row = (cv - K + k + H) * AP + (cu - K + H);
+                const float ar = valid ? __uint_as_float(q.z) * gv : 0.0f;
+                const float ai = valid ? __uint_as_float(q.w) * gv : 0.0f;
+                const bool chg = valid && (cu != pcu || cv != pcv);
+                if (__any_sync(0xFFFFFFFFu, chg)) {
+                    // the run ended: add its window row to the tile, restart
+                    const int row = pcv - K + k;
+                    const int col0 = pcu - K;
+                    const bool rin = chg && row >= 0 && row < T;
+#pragma unroll
+                    for (int j = 0; j < NT; j++) {
+                        if (rin && (unsigned)(col0 + j) < (unsigned)T) {
+                            atomicAdd(are + row * TP + col0 + j, acc_r[j]);
+                            atomicAdd(aim + row * TP + col0 + j, acc_i[j]);
+                        }
+                        acc_r[j] = chg ? 0 : acc_r[j];
+                        acc_i[j] = chg ? 0 : acc_i[j];
+                    }
+                }
+                if (valid) {
+                    pcu = cu;
+                    pcv = cv;
+                }
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
                     const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * NT + j);
-                    if (valid) {
-                        // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds
-                        // it to an integer held in the low mantissa bits
-                        atomicAdd(are + row + j,
-                                  __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits);
-                        atomicAdd(aim + row + j,
-                                  __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits);
+                    // |ar*g| < 2^22: adding 1.5*2^23 in the same FMA rounds it
+                    // to an integer held in the low mantissa bits
+                    acc_r[j] += __float_as_int(fmaf(ar, g, kRoundMagic)) - kRoundMagicBits;
+                    acc_i[j] += __float_as_int(fmaf(ai, g, kRoundMagic)) - kRoundMagicBits;
+                }
+            }
+            {
+                const int row = pcv - K + k;
+                const int col0 = pcu - K;
+                if (lane_on && row >= 0 && row < T) {
+#pragma unroll
+                    for (int j = 0; j < NT; j++) {
+                        if ((unsigned)(col0 + j) < (unsigned)T) {
+                            atomicAdd(are + row * TP + col0 + j, acc_r[j]);
+                            atomicAdd(aim + row * TP + col0 + j, acc_i[j]);
+                        }
                     }
                 }
             }
         }
         __syncthreads();
-        // write the interior (to the grid, or to this item's partial slot) and clear it
+        // write the tile (to the grid, or to this item's partial slot) and clear it
         const size_t gbase = (size_t)w * a.g.ny;
         const bool to_grid = !(is_split && chunk > 0);
         float2 *dst = to_grid ? grid
                               : parts + (size_t)(a.b.slot[bin] + chunk - 1) * (size_t)(T * T);
 #pragma unroll 4
         for (int i = 0; i < CPT; i++) {
-            const int c = tid + i * kThreads;
+            const int c = tid + i * kThreadsR;
             const int y = c / T, x = c % T;
-            const int idx = (y + H) * AP + x + H;
-            const float2 v = make_float2((float)are[idx] * inv, (float)aim[idx] * inv);
-            are[idx] = 0;
-            aim[idx] = 0;
+            const int ac = y * TP + x;
+            const float2 v = make_float2((float)are[ac] * inv, (float)aim[ac] * inv);
+            are[ac] = 0;
+            aim[ac] = 0;
             if (to_grid) {
                 if (x < tx && y < ty)
                     __stcg(grid + (gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x), v);
@@ -290,7 +444,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_grid_f32c(GridArgs a)
         __threadfence();
         const float2 *src = parts + (size_t)a.b.slot[bin] * (size_t)(T * T);
         for (int i = 0; i < CPT; i++) {
-            const int c = tid + i * kThreads;
+            const int c = tid + i * kThreadsR;
             const int y = c / T, x = c % T;
             if (x >= tx || y >= ty) continue;
             float2 *cell = grid + (gbase + (size_t)(v0 + y)) * a.g.nx + (size_t)(u0 + x);
@@ -503,9 +657,8 @@ __global__ void __launch_bounds__(kThreadsG64, 2) k_grid_f64(GridArgs a)
 template <int T, int K> size_t grid_smem(int prec)
 {
     if (prec == WSG_FP64) return (size_t)2 * T * (T + 2 * K + 1) * sizeof(double);
-    constexpr int AW = T + 4 * K;
-    constexpr int AP = AW | 1;
-    return ((size_t)(2 * AW * AP * 4) + 15) / 16 * 16 + (size_t)kStage * sizeof(uint4);
+    return acc_bytes<T>() + (size_t)kStageR * sizeof(uint4) + (size_t)T * T / 2 * 4 +
+           (size_t)kStageR * sizeof(unsigned short);
 }
 
 template <int T, int K> const void *grid_kernel(int prec)
@@ -547,22 +700,22 @@ int grid_max_ctas_per_sm(int prec, int tile, int half)
         return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, k, prec == WSG_FP64 ? kThreadsG64 : kThreads, smem) != cudaSuccess)
+            &nb, k, prec == WSG_FP64 ? kThreadsG64 : f32c_threads(half), smem) != cudaSuccess)
         return 0;
     return nb;
 }
 
 cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b, const RecBuffers &r,
-                        void *grid, void *partials, int ctas, cudaStream_t s)
+                        void *grid, void *partials, int ctas, cudaStream_t s, bool sparse)
 {
     size_t smem = 0;
     const void *k = grid_pick(prec, g.tile, g.half, smem);
     if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    GridArgs a{g, b, r, grid, partials};
+    GridArgs a{g, b, r, grid, partials, (sparse && prec == WSG_FP32C) ? 1 : 0};
     void *args[] = {&a};
-    return cudaLaunchKernel(k, dim3(ctas), dim3(prec == WSG_FP64 ? kThreadsG64 : kThreads), args,
+    return cudaLaunchKernel(k, dim3(ctas), dim3(prec == WSG_FP64 ? kThreadsG64 : f32c_threads(g.half)), args,
                             smem, s);
 }
 

@@ -38,7 +38,8 @@ constexpr int kThreads = 256;        // threads per CTA for tile kernels
 constexpr int kScanThreads = 256;    // bin-size scan: threads per CTA
 constexpr int kScanPerBlock = 4096;  // bin-size scan: bins per CTA
 constexpr int kStage = 512;          // records staged in shared memory per pass
-constexpr int kDefaultSplit = 4096;  // records per work item of a split bin
+constexpr int kDefaultSplit = 4096;      // records per work item of a split bin (FP64)
+constexpr int kDefaultSplitF32 = 16384;  // the same for FP32C plans
 
 struct DevCounters {
     unsigned long long records;
@@ -50,6 +51,7 @@ struct DevCounters {
     unsigned int error;
     unsigned int nsplit_items;   // work items of split bins (the list `split`)
     unsigned int nslots;         // partial tiles needed by split bins
+    unsigned int nwork;          // occupied bins that are not split (the list `work`)
 };
 
 // Geometry of the coordinate step (w-stacking.cu:66-77) and the tiling.
@@ -66,18 +68,21 @@ struct GeomParams {
 // Work decomposition.  A bin with more than `split` records is cut into
 // ceil(n/split) work items of at most `split` records; they are listed in
 // `split` (entry = bin | chunk << 32) and processed first.  Every other bin is
-// one work item.
+// one work item; the occupied ones among them are also listed in `work` (in
+// no particular order), for kernels that skip empty bins.
 //
 // Counting uses nsub sub-counters per bin (nsub = kSub for plans, 1 for the
-// no-allocation entry point; a power of two): measurement m uses sub-counter
-// (m >> 8) % nsub in both passes, which spreads the atomics of crowded bins
-// over nsub addresses.  After the scan, sub_prim[s][b] / sub_dup[s][b] hold
-// the first record position of sub-range s of bin b's primaries / duplicates
-// and the scatter advances them as cursors.
-constexpr int kSub = 8;
+// no-allocation entry point): a record uses the sub-counter of the 4x4 block
+// (in Morton order) that holds its tile-relative cell, clamped to the tile, in
+// both passes.  A bin's records are then grouped block by block, which keeps
+// each sorted stage of the FP32C gridder within a compact area, and the
+// atomics of a crowded bin are spread over nsub addresses.  After the scan,
+// sub_prim[s][b] / sub_dup[s][b] hold the first record position of sub-range s
+// of bin b's primaries / duplicates and the scatter advances them as cursors.
+constexpr int kSub = 16;
 struct BinBuffers {
     unsigned *sub_prim, *sub_dup;            // [nsub][nbins]
-    unsigned *off, *nprim, *ntotal, *is_split, *slot, *done;   // [nbins]
+    unsigned *off, *nprim, *ntotal, *is_split, *slot, *done, *work;   // [nbins]
     unsigned long long *part;                // 2 * scan_blocks(nbins) entries
     unsigned long long *split;               // split-item list
     DevCounters *ctr;
@@ -98,10 +103,10 @@ struct RecBuffers {
 
 // Bytes of BinBuffers storage for nbins bins with nsub sub-counters and at
 // most `items` split items (u32 arrays, then the scan partials, then the
-// split list; 256-byte aligned): (2*nsub + 6)*4 bytes per bin, 16 per 4096
+// split list; 256-byte aligned): (2*nsub + 7)*4 bytes per bin, 16 per 4096
 // bins and 8 per split item.
 long long scan_blocks(long long nbins);
-inline size_t bin_u32_per_bin(unsigned nsub) { return 2 * (size_t)nsub + 6; }
+inline size_t bin_u32_per_bin(unsigned nsub) { return 2 * (size_t)nsub + 7; }
 inline size_t bin_buffer_bytes(long long nbins, unsigned long long items, unsigned nsub)
 {
     const size_t a = (bin_u32_per_bin(nsub) * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
@@ -121,6 +126,7 @@ inline void bin_buffer_carve(void *base, long long nbins, unsigned nsub, BinBuff
     b.is_split = v + 3 * nbins;
     b.slot = v + 4 * nbins;
     b.done = v + 5 * nbins;
+    b.work = v + 6 * nbins;
     unsigned char *c = reinterpret_cast<unsigned char *>(base);
     const size_t a = (bin_u32_per_bin(nsub) * nbins * sizeof(unsigned) + 255) & ~(size_t)255;
     const size_t p = ((size_t)scan_blocks(nbins) * 16 + 255) & ~(size_t)255;
@@ -186,9 +192,12 @@ cudaError_t launch_bin_scatter_batch(const GeomParams &g, int prec, const ChanTa
 // ---- launchers (grid.cu) ----
 // partials: FP32C partial tiles of split bins (max_slots * tile^2 float2),
 // unused for FP64.
+// sparse: FP32C only; grids the occupied bins alone and leaves the tiles of
+// empty bins unwritten (for the fused imaging path, whose column transforms
+// read occupied tiles only).  Otherwise every tile of the grid is written.
 cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b,
                         const RecBuffers &r, void *grid, void *partials, int ctas,
-                        cudaStream_t s);
+                        cudaStream_t s, bool sparse = false);
 int grid_max_ctas_per_sm(int prec, int tile, int half);
 
 // ---- launchers (degrid.cu) ----

@@ -55,6 +55,23 @@ def test_pruned_fused_forward_equals_dense(gpu):
     assert _rel_rms(a, b) <= 2e-6
 
 
+def test_occupied_tiles_grid_feeds_the_pruned_forward(gpu):
+    """wsg_grid_occupied writes the occupied tiles exactly as wsg_grid does and
+    leaves the others untouched; with pruning the forward reads no others."""
+    import torch
+    p, obs = _gridded_plan("fp32c")
+    dense = p.grid()
+    poisoned = torch.full_like(dense, complex(float("nan"), float("nan")))
+    occ = p.grid(poisoned, occupied_only=True)
+    assert torch.isnan(occ.real).any()            # empty tiles left as they were
+    finite = ~torch.isnan(occ.real)
+    assert torch.equal(occ[finite], dense[finite])
+    assert float(dense[~finite].abs().max()) == 0.0
+    a = p.fft_wcorrect(occ, prune=True).cpu().numpy()
+    b = p.fft_wcorrect(dense.clone(), prune=True).cpu().numpy()
+    assert np.array_equal(a, b)
+
+
 def test_pruned_fused_adjoint_equals_dense_on_degridded_cells(gpu):
     import torch
     p, obs = _gridded_plan("fp32c")
