@@ -325,10 +325,10 @@ WSG_API long long wsg_batch_device_bytes(wsg_batch *batch);
  * `stream` (a cudaStream_t, NULL = legacy default stream).
  * Its scratch is a fixed 64 MiB static device array per GPU, held until the
  * process exits; a call needing more than
- *     2560 + 32*nbins + 16*ceil(nbins/4096) + 161*num_points bytes
+ *     2560 + 36*nbins + 16*ceil(nbins/256) + 161*num_points bytes
  *     (alignment included),
  *     nbins = num_w_planes*ceil(grid_size_y/64)*ceil(grid_size_x/64),
- * fails with WSG_ERR_CAPACITY (about 390,000 measurements on a 4096x4096x32
+ * fails with WSG_ERR_CAPACITY (about 387,000 measurements on a 4096x4096x32
  * grid).  Each call overwrites the whole grid: a larger set is gridded part by
  * part into separate grids that the caller sums.  All calls share that array: calls whose GPU work may overlap race
  * and must be serialised by the caller.  The first call on a device looks up

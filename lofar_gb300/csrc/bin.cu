@@ -64,16 +64,38 @@ __device__ __forceinline__ int measure(const GeomParams &g, double x, double y, 
     return 0;
 }
 
+// measure() without the fractions: the status and the geometry only.
+template <bool UP2, bool WP2>
+__device__ __forceinline__ int measure_cells(const GeomParams &g, double x, double y, double z,
+                                             MGeom &o)
+{
+    bool oku, okv, okw;
+    const int cu = coord_cell<UP2>(x, g.ku, g.dx, oku);
+    const int cv = coord_cell<UP2>(y, g.ku, g.dx, okv);
+    const int cw = coord_cell<WP2>(z, g.kw, g.dw, okw);
+    if (!oku || !okv) return 2;
+    const int K = g.half;
+    const int ju0 = max(cu - K, 0), ju1 = min(cu + K, g.nx - 1);
+    const int jv0 = max(cv - K, 0), jv1 = min(cv + K, g.ny - 1);
+    if (ju0 > ju1 || jv0 > jv1) return 2;
+    if (!okw || cw < 0 || cw >= g.wplanes) return 1;
+    o.gu = cu;
+    o.gv = cv;
+    o.gw = cw;
+    o.tu0 = ju0 >> g.tile_shift;
+    o.tu1 = ju1 >> g.tile_shift;
+    o.tv0 = jv0 >> g.tile_shift;
+    o.tv1 = jv1 >> g.tile_shift;
+    o.tup = min(max(cu, 0), g.nx - 1) >> g.tile_shift;
+    o.tvp = min(max(cv, 0), g.ny - 1) >> g.tile_shift;
+    return 0;
+}
+
 __device__ __forceinline__ unsigned bin_index(const GeomParams &g, int w, int tv, int tu)
 {
     return (unsigned)(((long long)w * g.ntv + tv) * g.ntu + tu);
 }
 
-// Both passes give each thread kItems measurements per sweep (item i of a
-// thread at base + i*blockDim + tid, so each item slot is a coalesced load);
-// their loads and atomics are independent, which keeps several memory
-// operations in flight per thread.
-constexpr int kItems = 4;
 
 // Sub-range of a record within its bin: the 4x4 block (T/4 cells square) of
 // its tile-relative cell, clamped to the tile, in Morton order; one range
@@ -89,45 +111,110 @@ __device__ __forceinline__ unsigned sub_key(const GeomParams &g, unsigned nsub, 
     return (bx & 1u) | ((by & 1u) << 1) | ((bx & 2u) << 1) | ((by & 2u) << 2);
 }
 
+// Both passes give each thread IT measurements per tile of 256*IT: item i of
+// thread t of tile q is measurement 256*IT*q + 256*i + t (coalesced loads).
+template <int IT>
+__device__ __forceinline__ long long tile_m(long long q, int i)
+{
+    return q * (256 * IT) + (long long)i * 256 + threadIdx.x;
+}
+
+// The counters of a measurement's records, one per tile of its window's 2x2
+// tile block (d: du = d & 1, dv = d >> 1 from (tu0, tv0)): indices into the
+// counter array sub_prim, which sub_dup follows (primaries, then duplicates);
+// kFull where the window has no tile.  dp: the primary's d.
+__device__ __forceinline__ void rec_keys(const GeomParams &g, const BinBuffers &b, const MGeom &o,
+                                         int st, unsigned nb, unsigned key[4], int &dp)
+{
+    dp = 0;
+    if (st != 0) {
+        key[0] = key[1] = key[2] = key[3] = kFull;
+        return;
+    }
+    const unsigned b0 = ((unsigned)o.gw * (unsigned)g.ntv + (unsigned)o.tv0) * (unsigned)g.ntu +
+                        (unsigned)o.tu0;
+    const int t1 = g.tile - 1, bs = g.tile_shift - 2;
+    const int cu0 = o.gu - (o.tu0 << g.tile_shift), cv0 = o.gv - (o.tv0 << g.tile_shift);
+    const unsigned bx0 = (unsigned)min(max(cu0, 0), t1) >> bs;
+    const unsigned bx1 = (unsigned)min(max(cu0 - g.tile, 0), t1) >> bs;
+    const unsigned by0 = (unsigned)min(max(cv0, 0), t1) >> bs;
+    const unsigned by1 = (unsigned)min(max(cv0 - g.tile, 0), t1) >> bs;
+    const bool two_u = o.tu1 > o.tu0, two_v = o.tv1 > o.tv0;
+    dp = (o.tup - o.tu0) | ((o.tvp - o.tv0) << 1);
+    const unsigned dupbase = b.nsub * nb;
+#pragma unroll
+    for (int d = 0; d < 4; d++) {
+        const int du = d & 1, dv = d >> 1;
+        const bool has = (du == 0 || two_u) && (dv == 0 || two_v);
+        const unsigned bx = du ? bx1 : bx0, by = dv ? by1 : by0;
+        const unsigned sub = b.nsub >= 16u
+                                 ? (bx & 1u) | ((by & 1u) << 1) | ((bx & 2u) << 1) | ((by & 2u) << 2)
+                                 : 0u;
+        key[d] = has ? (d == dp ? 0u : dupbase) + sub * nb + b0 + (unsigned)(dv * g.ntu + du) : kFull;
+    }
+}
+
+// Runs of equal keys in consecutive lanes: the run's first lane (`lead`), its
+// length (`cnt`, valid at the lead) and this lane's rank in it.  A key that
+// recurs after a different one starts a new run, so runs are exact and each
+// run takes its own cursor atomic.
+__device__ __forceinline__ void warp_runs(unsigned key, int lane, int &lead, unsigned &cnt,
+                                          unsigned &rank)
+{
+    const unsigned prev = __shfl_up_sync(kFull, key, 1);
+    const unsigned heads = __ballot_sync(kFull, lane == 0 || prev != key);
+    const unsigned upto = lane == 31 ? kFull : ((2u << lane) - 1u);
+    lead = 31 - __clz(heads & upto);
+    const unsigned after = heads & ~upto;
+    const int next = after ? __ffs(after) - 1 : 32;
+    cnt = (unsigned)(next - lane);   // run length when lane == lead
+    rank = (unsigned)(lane - lead);
+}
+
+constexpr int kItemsCount = 4;     // measurements a thread per tile, counting pass
+constexpr int kItemsScatter = 2;   // the same, scatter pass (registers)
+
+// Counting pass.  Primaries take one atomic per run of equal counters in
+// consecutive lanes (crowded bins near the uv origin are hit by neighbouring
+// measurements); duplicates, which lie along tile edges, one atomic each.
 template <bool UP2, bool WP2>
 __global__ void __launch_bounds__(256)
 k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
-            const double *__restrict__ ww, long long n, BinBuffers b)
+            const double *__restrict__ ww, long long n, long long tiles, BinBuffers b)
 {
+    constexpr int IT = kItemsCount;
     const int lane = threadIdx.x & 31;
-    const long long stride = (long long)gridDim.x * blockDim.x * kItems;
-    const long long nb = g.nbins;
-    for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
-        double x[kItems], y[kItems], z[kItems];
+    const unsigned nb = (unsigned)g.nbins;
+    for (long long q = blockIdx.x; q < tiles; q += gridDim.x) {
+        double x[IT], y[IT], z[IT];
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+        for (int i = 0; i < IT; i++) {
+            const long long m = tile_m<IT>(q, i);
             x[i] = m < n ? __ldcs(uu + m) : 0.0;
             y[i] = m < n ? __ldcs(vv + m) : 0.0;
             z[i] = m < n ? __ldcs(ww + m) : 0.0;
         }
         int ndp = 0, ndw = 0;
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+        for (int i = 0; i < IT; i++) {
+            const long long m = tile_m<IT>(q, i);
             MGeom o;
-            float fu, fv;
-            const int st = m < n ? measure<UP2, WP2, float>(g, x[i], y[i], z[i], o, fu, fv) : 3;
+            const int st = m < n ? measure_cells<UP2, WP2>(g, x[i], y[i], z[i], o) : 3;
             ndp += st == 1;
             ndw += st == 2;
-            // primaries: one aggregated atomic per (sub-range, bin) and warp
-            const unsigned prim = (st == 0) ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) * nb +
-                                                  bin_index(g, o.gw, o.tvp, o.tup)
-                                            : kFull;
-            const unsigned peers = __match_any_sync(kFull, prim);
-            if (st == 0) {
-                if (lane == __ffs(peers) - 1) atomicAdd(&b.sub_prim[prim], (unsigned)__popc(peers));
-                for (int tv = o.tv0; tv <= o.tv1; tv++)
-                    for (int tu = o.tu0; tu <= o.tu1; tu++)
-                        if (tv != o.tvp || tu != o.tup)
-                            atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb +
-                                                 bin_index(g, o.gw, tv, tu)], 1u);
-            }
+            unsigned key[4];
+            int dp;
+            rec_keys(g, b, o, st, nb, key, dp);
+            unsigned kp = kFull;
+#pragma unroll
+            for (int d = 0; d < 4; d++) kp = d == dp ? key[d] : kp;
+            int lead;
+            unsigned cnt, rank;
+            warp_runs(kp, lane, lead, cnt, rank);
+            if (kp != kFull && lane == lead) atomicAdd(&b.sub_prim[kp], cnt);
+#pragma unroll
+            for (int d = 0; d < 4; d++)
+                if (d != dp && key[d] != kFull) atomicAdd(&b.sub_prim[key[d]], 1u);
         }
         for (int d = 16; d >= 1; d >>= 1) {
             ndp += __shfl_xor_sync(kFull, ndp, d);
@@ -180,23 +267,22 @@ __global__ void __launch_bounds__(256)
 k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
               const double *__restrict__ ww, const float *__restrict__ vr,
               const float *__restrict__ vi, const float *__restrict__ wt, long long n,
-              long long nf, long long np, BinBuffers b, RecBuffers r)
+              long long tiles, long long nf, long long np, BinBuffers b, RecBuffers r)
 {
     using S = typename std::conditional<PREC == WSG_FP64, double, float>::type;
+    constexpr int IT = kItemsScatter;
     const int lane = threadIdx.x & 31;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    const long long stride = (long long)gridDim.x * blockDim.x * kItems;
-    const long long nb = g.nbins;
+    const unsigned nb = (unsigned)g.nbins;
     // one frequency and one polarisation (the usual case): the value is one
     // float product, and its inputs are loaded with the coordinates so that
     // their latency overlaps the cursor atomics
     const bool single = nf == 1 && np == 1;
-    for (long long base = (long long)blockIdx.x * blockDim.x * kItems; base < n; base += stride) {
-        double x[kItems], y[kItems], z[kItems];
-        float a_re[kItems], a_im[kItems], a_wt[kItems];
+    for (long long q = blockIdx.x; q < tiles; q += gridDim.x) {
+        double x[IT], y[IT], z[IT];
+        float a_re[IT], a_im[IT], a_wt[IT];
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+        for (int i = 0; i < IT; i++) {
+            const long long m = tile_m<IT>(q, i);
             x[i] = m < n ? __ldcs(uu + m) : 0.0;
             y[i] = m < n ? __ldcs(vv + m) : 0.0;
             z[i] = m < n ? __ldcs(ww + m) : 0.0;
@@ -204,31 +290,55 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             a_im[i] = (single && m < n) ? __ldcs(vi + m) : 0.0f;
             a_wt[i] = (single && m < n) ? __ldcs(wt + m) : 0.0f;
         }
-        // primary positions first (one aggregated cursor atomic per bin and warp)
-        unsigned ppos[kItems];
+        // record positions first: every cursor atomic of the tile is issued
+        // before the first result is used.  Primaries take one atomic per run
+        // of equal counters in consecutive lanes, duplicates one each.
+        unsigned pos[IT][4];   // duplicates (the primary's entry unused)
+        unsigned ppos[IT];     // primary: the run's base at the lead lane, then its position
+        unsigned lr[IT];
+        int dpi[IT];
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+        for (int i = 0; i < IT; i++) {
+            const long long m = tile_m<IT>(q, i);
             MGeom o;
-            S fu, fv;
-            const int st = m < n ? measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv) : 3;
-            const unsigned prim = (st == 0) ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) * nb +
-                                                  bin_index(g, o.gw, o.tvp, o.tup)
-                                            : kFull;
-            const unsigned peers = __match_any_sync(kFull, prim);
-            const int leader = __ffs(peers) - 1;
-            unsigned got = 0;
-            if (st == 0 && lane == leader) got = atomicAdd(&b.sub_prim[prim], (unsigned)__popc(peers));
-            const unsigned basep = __shfl_sync(kFull, got, leader);
-            ppos[i] = (st == 0) ? basep + (unsigned)__popc(peers & lt_mask) : 0xFFFFFFFFu;
+            const int st = m < n ? measure_cells<UP2, WP2>(g, x[i], y[i], z[i], o) : 3;
+            unsigned key[4];
+            rec_keys(g, b, o, st, nb, key, dpi[i]);
+            unsigned kp = kFull;
+#pragma unroll
+            for (int d = 0; d < 4; d++) kp = d == dpi[i] ? key[d] : kp;
+            int lead;
+            unsigned cnt, rank;
+            warp_runs(kp, lane, lead, cnt, rank);
+            lr[i] = ((unsigned)lead << 8) | rank;
+            ppos[i] = (kp != kFull && lane == lead) ? atomicAdd(&b.sub_prim[kp], cnt) : 0u;
+            if (kp == kFull) lr[i] |= 0x80000000u;   // no record
+#pragma unroll
+            for (int d = 0; d < 4; d++)
+                pos[i][d] = (d != dpi[i] && key[d] != kFull) ? atomicAdd(&b.sub_prim[key[d]], 1u)
+                                                              : kFull;
+        }
+        // the primary's run base comes from its lead lane
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const unsigned base = __shfl_sync(kFull, ppos[i], (int)((lr[i] >> 8) & 31u));
+            ppos[i] = (lr[i] & 0x80000000u) ? kFull : base + (lr[i] & 0xFFu);
         }
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-            if (ppos[i] == 0xFFFFFFFFu) continue;
-            const long long m = base + (long long)i * blockDim.x + threadIdx.x;
+        for (int i = 0; i < IT; i++) {
+            if (ppos[i] == kFull) continue;   // a measurement with records has a primary
+            const long long m = tile_m<IT>(q, i);
             MGeom o;
-            S fu, fv;
-            measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv);
+            S fu = 0, fv = 0;
+            unsigned qu = 0u, qv = 0u;
+            if (PREC == WSG_FP64) {
+                measure<UP2, WP2, S>(g, x[i], y[i], z[i], o, fu, fv);
+            } else {
+                measure_cells<UP2, WP2>(g, x[i], y[i], z[i], o);
+                bool ok;
+                coord_cell_q24<UP2>(x[i], g.ku, g.dx, qu, ok);
+                coord_cell_q24<UP2>(y[i], g.ku, g.dx, qv, ok);
+            }
             S re, im;
             if (single) {
                 // the fold of w-stacking.cu:98-112 with one entry
@@ -237,27 +347,24 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             } else {
                 fold_value<S>(vr, vi, wt, m, nf, np, re, im);
             }
-            for (int tv = o.tv0; tv <= o.tv1; tv++) {
-                for (int tu = o.tu0; tu <= o.tu1; tu++) {
-                    const unsigned bin = bin_index(g, o.gw, tv, tu);
-                    const unsigned pos =
-                        (tv == o.tvp && tu == o.tup)
-                            ? ppos[i]
-                            : atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb + bin], 1u);
-                    const int cu = o.gu - (tu << g.tile_shift);
-                    const int cv = o.gv - (tv << g.tile_shift);
-                    if (PREC == WSG_FP64) {
-                        r.cell[pos] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
-                        reinterpret_cast<double2 *>(r.frac)[pos] = make_double2(fu, fv);
-                        reinterpret_cast<double2 *>(r.val)[pos] = make_double2(re, im);
-                    } else {
-                        r.rec16[pos] = make_uint4(pack_axis(cu, (float)fu), pack_axis(cv, (float)fv),
-                                                  __float_as_uint((float)re),
-                                                  __float_as_uint((float)im));
-                    }
-                    // only the degridder reads idx, and only of primaries
-                    if (tv == o.tvp && tu == o.tup) r.idx[pos] = (unsigned)m;
+#pragma unroll
+            for (int d = 0; d < 4; d++) {
+                const unsigned p = d == dpi[i] ? ppos[i] : pos[i][d];
+                if (p == kFull) continue;
+                const int tu = o.tu0 + (d & 1), tv = o.tv0 + (d >> 1);
+                const int cu = o.gu - (tu << g.tile_shift);
+                const int cv = o.gv - (tv << g.tile_shift);
+                if (PREC == WSG_FP64) {
+                    r.cell[p] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
+                    reinterpret_cast<double2 *>(r.frac)[p] = make_double2(fu, fv);
+                    reinterpret_cast<double2 *>(r.val)[p] = make_double2(re, im);
+                } else {
+                    r.rec16[p] = make_uint4(((unsigned)(cu + 64) << 24) | qu,
+                                            ((unsigned)(cv + 64) << 24) | qv,
+                                            __float_as_uint((float)re), __float_as_uint((float)im));
                 }
+                // only the degridder reads idx, and only of primaries
+                if (tu == o.tup && tv == o.tvp) r.idx[p] = (unsigned)m;
             }
         }
     }
@@ -613,11 +720,9 @@ __global__ void __launch_bounds__(kScanThreads) k_bin_scan_c(long long nbins, Bi
     }
 }
 
-int stream_grid(long long n, int threads)
+int tile_grid(long long tiles)
 {
-    const long long want = (n + (long long)threads * kItems - 1) / ((long long)threads * kItems);
-    const long long cap = (long long)num_sms() * 8;
-    return (int)max(1ll, min(want, cap));
+    return (int)max(1ll, min(tiles, (long long)num_sms() * 8));
 }
 
 }  // namespace
@@ -628,11 +733,12 @@ cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double
                              const double *ww, long long n, const BinBuffers &b, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    const int blocks = stream_grid(n, 256);
-    if (g.u_pow2 && g.w_pow2) k_bin_count<true, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, b);
-    else if (g.u_pow2) k_bin_count<true, false><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, b);
-    else if (g.w_pow2) k_bin_count<false, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, b);
-    else k_bin_count<false, false><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, b);
+    const long long tiles = (n + 256 * kItemsCount - 1) / (256 * kItemsCount);
+    const int blocks = tile_grid(tiles);
+    if (g.u_pow2 && g.w_pow2) k_bin_count<true, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, tiles, b);
+    else if (g.u_pow2) k_bin_count<true, false><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, tiles, b);
+    else if (g.w_pow2) k_bin_count<false, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, tiles, b);
+    else k_bin_count<false, false><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, tiles, b);
     return cudaGetLastError();
 }
 
@@ -651,15 +757,16 @@ static void scatter_dispatch(const GeomParams &g, const double *uu, const double
                              const float *wt, long long n, long long nf, long long np,
                              const BinBuffers &b, const RecBuffers &r, cudaStream_t s)
 {
-    const int blocks = stream_grid(n, 256);
+    const long long tiles = (n + 256 * kItemsScatter - 1) / (256 * kItemsScatter);
+    const int blocks = tile_grid(tiles);
     if (g.u_pow2 && g.w_pow2)
-        k_bin_scatter<true, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<true, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, tiles, nf, np, b, r);
     else if (g.u_pow2)
-        k_bin_scatter<true, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<true, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, tiles, nf, np, b, r);
     else if (g.w_pow2)
-        k_bin_scatter<false, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<false, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, tiles, nf, np, b, r);
     else
-        k_bin_scatter<false, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, nf, np, b, r);
+        k_bin_scatter<false, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, n, tiles, nf, np, b, r);
 }
 
 cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu, const double *vv,

@@ -138,7 +138,7 @@ int wsg::plan_configure(wsg_plan *p)
     g.ku = g.u_pow2 ? k : 0;
     g.w_pow2 = is_pow2_recip(p->dw, k) ? 1 : 0;
     g.kw = g.w_pow2 ? k : 0;
-    if (g.nbins * kSub >= (1ll << 32) - 1)
+    if (g.nbins * 2 * kSub >= (1ll << 32) - 1)
         return set_error(WSG_ERR_UNSUPPORTED, "too many (plane, tile) bins: %lld", g.nbins);
     const int sms = num_sms();
     const int og = grid_max_ctas_per_sm(p->prec, p->tile, p->half);

@@ -132,4 +132,59 @@ __device__ __forceinline__ Cell<F> coord_step(double x, int k, double d)
     return c;
 }
 
+// The cell alone, cell = (int)(x/d).  With a power-of-two d = 2^-k and a
+// non-negative normal x whose x * 2^k has its integer part in the high word of
+// the mantissa (1075 - e - k in [33, 52], e the biased exponent: every x in
+// [2^-(k+20), 1) for k <= 20), the integer part is one shift of the high word;
+// other inputs take the general path.  Same result as coord_step's cell.
+template <bool POW2>
+__device__ __forceinline__ int coord_cell(double x, int k, double d, bool &ok)
+{
+    if (POW2) {
+        const unsigned hi = (unsigned)__double2hiint(x);
+        const int e = (int)((hi >> 20) & 0x7FFu);
+        const int sh = 1075 - e - k;
+        if ((hi >> 31) == 0u && e != 0 && sh >= 33 && sh <= 52) {
+            ok = true;
+            return (int)(((hi & 0xFFFFFu) | 0x100000u) >> (sh - 32));
+        }
+        const Split r = split_pow2(x, k);
+        ok = r.ok;
+        return (int)r.g;
+    }
+    const double pos = x / d;
+    ok = fabs(pos) < 1073741824.0;  // false for NaN
+    return ok ? (int)pos : 0;
+}
+
+// The cell and the fraction as the FP32C record stores it: q24 =
+// (frac + 1) * 2^23 rounded to an integer, at most 2^24 - 1.  On coord_cell's
+// fast path the fraction's bits are rounded once, to nearest even, straight
+// from the mantissa; otherwise the fraction is first rounded to a float.
+template <bool POW2>
+__device__ __forceinline__ int coord_cell_q24(double x, int k, double d, unsigned &q24, bool &ok)
+{
+    if (POW2) {
+        const unsigned hi = (unsigned)__double2hiint(x);
+        const int e = (int)((hi >> 20) & 0x7FFu);
+        const int sh = 1075 - e - k;
+        if ((hi >> 31) == 0u && e != 0 && sh >= 33 && sh <= 52) {
+            const unsigned lo = (unsigned)__double2loint(x);
+            const unsigned mh = (hi & 0xFFFFFu) | 0x100000u;
+            const unsigned fh = mh & ((1u << (sh - 32)) - 1u);   // fraction = fh:lo * 2^-sh
+            const int r = sh - 23;                               // in [10, 29]
+            const unsigned t = __funnelshift_r(lo, fh, r);       // floor(frac * 2^23) < 2^23
+            const unsigned rem = lo & ((1u << r) - 1u), half = 1u << (r - 1);
+            const unsigned up = (rem > half || (rem == half && (t & 1u))) ? 1u : 0u;
+            q24 = min((1u << 23) + t + up, 0xFFFFFFu);
+            ok = true;
+            return (int)(mh >> (sh - 32));
+        }
+    }
+    const Cell<float> c = coord_step<POW2, float>(x, k, d);
+    q24 = min((unsigned)__float2int_rn((c.frac + 1.0f) * 8388608.0f), 0xFFFFFFu);
+    ok = c.ok;
+    return c.g;
+}
+
 }  // namespace wsg

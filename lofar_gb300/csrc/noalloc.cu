@@ -12,11 +12,11 @@
 //
 // The array is a fixed 64 MiB of device memory per GPU that loads the library,
 // held until the process exits.  A call needs at most
-//     2560 + 32*nbins + 16*ceil(nbins/4096) + 161*num_points   bytes
+//     2560 + 36*nbins + 16*ceil(nbins/256) + 161*num_points   bytes
 //     (alignment padding included),
 //     nbins = num_w_planes * ceil(grid_size_y/64) * ceil(grid_size_x/64),
 // and is rejected with WSG_ERR_CAPACITY when that exceeds the array: for a
-// 4096x4096x32 grid that is about 390,000 measurements per call.  Every call
+// 4096x4096x32 grid that is about 387,000 measurements per call.  Every call
 // overwrites the whole grid (as wstack() does), so a caller splitting a larger
 // set grids each part into its own grid and sums the grids.  Its bin table
 // keeps one counter per bin and kind (no sub-counters).
@@ -178,7 +178,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     const size_t need = o_val + up256(cap * sizeof(double2));
     if (g.nbins >= (1ll << 31) || need > kNoAllocBytes)
         return fail(WSG_ERR_CAPACITY,
-                    "wsg_grid_noalloc: needs %zu bytes of scratch (about 32*%lld bins + 161*%ld "
+                    "wsg_grid_noalloc: needs %zu bytes of scratch (about 36*%lld bins + 161*%ld "
                     "measurements), above its fixed %zu-byte array; every call overwrites the "
                     "whole grid, so grid the parts into separate grids and sum them, or use "
                     "the plan API",

@@ -36,7 +36,7 @@ constexpr double kRefPi = 3.14159265359;
 constexpr int kMaxHalf = 7;          // support up to 15 cells
 constexpr int kThreads = 256;        // threads per CTA for tile kernels
 constexpr int kScanThreads = 256;    // bin-size scan: threads per CTA
-constexpr int kScanPerBlock = 4096;  // bin-size scan: bins per CTA
+constexpr int kScanPerBlock = 256;   // bin-size scan: bins per CTA (one a thread)
 constexpr int kStage = 512;          // records staged in shared memory per pass
 constexpr int kDefaultSplit = 4096;      // records per work item of a split bin (FP64)
 constexpr int kDefaultSplitF32 = 16384;  // the same for FP32C plans
@@ -103,7 +103,7 @@ struct RecBuffers {
 
 // Bytes of BinBuffers storage for nbins bins with nsub sub-counters and at
 // most `items` split items (u32 arrays, then the scan partials, then the
-// split list; 256-byte aligned): (2*nsub + 7)*4 bytes per bin, 16 per 4096
+// split list; 256-byte aligned): (2*nsub + 7)*4 bytes per bin, 16 per 256
 // bins and 8 per split item.
 long long scan_blocks(long long nbins);
 inline size_t bin_u32_per_bin(unsigned nsub) { return 2 * (size_t)nsub + 7; }
