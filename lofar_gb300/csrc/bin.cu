@@ -97,18 +97,14 @@ __device__ __forceinline__ unsigned bin_index(const GeomParams &g, int w, int tv
 }
 
 
-// Sub-range of a record within its bin: the 4x4 block (T/4 cells square) of
-// its tile-relative cell, clamped to the tile, in Morton order; one range
-// when nsub < 16.  The tile kernels then meet a bin's records block by block,
-// so each of their sorted stages covers a compact area.
-__device__ __forceinline__ unsigned sub_key(const GeomParams &g, unsigned nsub, int cell_u,
-                                            int cell_v, int tu, int tv)
+// Sub-range of a record within its bin: the measurement's cell modulo 4 in
+// each axis; one range when nsub < 16.  Every record of one cell falls in
+// one sub-range, so the tile kernels' sorted stages keep each cell's records
+// together, and the atomics of a crowded region of the grid are spread over
+// 16 counters.
+__device__ __forceinline__ unsigned sub_key(unsigned nsub, int cell_u, int cell_v)
 {
-    if (nsub < 16u) return 0u;
-    const int t1 = g.tile - 1;
-    const unsigned bx = (unsigned)min(max(cell_u - (tu << g.tile_shift), 0), t1) >> (g.tile_shift - 2);
-    const unsigned by = (unsigned)min(max(cell_v - (tv << g.tile_shift), 0), t1) >> (g.tile_shift - 2);
-    return (bx & 1u) | ((by & 1u) << 1) | ((bx & 2u) << 1) | ((by & 2u) << 2);
+    return nsub >= 16u ? ((unsigned)cell_u & 3u) | (((unsigned)cell_v & 3u) << 2) : 0u;
 }
 
 // Both passes give each thread IT measurements per tile of 256*IT: item i of
@@ -132,13 +128,7 @@ __device__ __forceinline__ void rec_keys(const GeomParams &g, const BinBuffers &
         return;
     }
     const unsigned b0 = ((unsigned)o.gw * (unsigned)g.ntv + (unsigned)o.tv0) * (unsigned)g.ntu +
-                        (unsigned)o.tu0;
-    const int t1 = g.tile - 1, bs = g.tile_shift - 2;
-    const int cu0 = o.gu - (o.tu0 << g.tile_shift), cv0 = o.gv - (o.tv0 << g.tile_shift);
-    const unsigned bx0 = (unsigned)min(max(cu0, 0), t1) >> bs;
-    const unsigned bx1 = (unsigned)min(max(cu0 - g.tile, 0), t1) >> bs;
-    const unsigned by0 = (unsigned)min(max(cv0, 0), t1) >> bs;
-    const unsigned by1 = (unsigned)min(max(cv0 - g.tile, 0), t1) >> bs;
+                        (unsigned)o.tu0 + sub_key(b.nsub, o.gu, o.gv) * nb;
     const bool two_u = o.tu1 > o.tu0, two_v = o.tv1 > o.tv0;
     dp = (o.tup - o.tu0) | ((o.tvp - o.tv0) << 1);
     const unsigned dupbase = b.nsub * nb;
@@ -146,11 +136,7 @@ __device__ __forceinline__ void rec_keys(const GeomParams &g, const BinBuffers &
     for (int d = 0; d < 4; d++) {
         const int du = d & 1, dv = d >> 1;
         const bool has = (du == 0 || two_u) && (dv == 0 || two_v);
-        const unsigned bx = du ? bx1 : bx0, by = dv ? by1 : by0;
-        const unsigned sub = b.nsub >= 16u
-                                 ? (bx & 1u) | ((by & 1u) << 1) | ((bx & 2u) << 1) | ((by & 2u) << 2)
-                                 : 0u;
-        key[d] = has ? (d == dp ? 0u : dupbase) + sub * nb + b0 + (unsigned)(dv * g.ntu + du) : kFull;
+        key[d] = has ? (d == dp ? 0u : dupbase) + b0 + (unsigned)(dv * g.ntu + du) : kFull;
     }
 }
 
@@ -172,7 +158,7 @@ __device__ __forceinline__ void warp_runs(unsigned key, int lane, int &lead, uns
 }
 
 constexpr int kItemsCount = 4;     // measurements a thread per tile, counting pass
-constexpr int kItemsScatter = 2;   // the same, scatter pass (registers)
+constexpr int kItemsScatter = 1;   // the same, scatter pass (registers, occupancy)
 
 // Counting pass.  Primaries take one atomic per run of equal counters in
 // consecutive lanes (crowded bins near the uv origin are hit by neighbouring
@@ -434,7 +420,7 @@ __global__ void __launch_bounds__(256) k_bin_count_batch(GeomParams g, ChanTable
         float fu, fv;
         BatchPoint bp;
         const int st = batch_point<UP2, WP2, float>(g, t, s_m0, m, o, fu, fv, bp);
-        const unsigned psub = st == 0 ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) : 0u;
+        const unsigned psub = st == 0 ? sub_key(b.nsub, o.gu, o.gv) : 0u;
         for (int p = 0; p < t.pols; p++) {
             const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
             const unsigned prim = (st == 0) ? psub * nb + bin_index(g, plane, o.tvp, o.tup) : kFull;
@@ -444,7 +430,7 @@ __global__ void __launch_bounds__(256) k_bin_count_batch(GeomParams g, ChanTable
                 for (int tv = o.tv0; tv <= o.tv1; tv++)
                     for (int tu = o.tu0; tu <= o.tu1; tu++)
                         if (tv != o.tvp || tu != o.tup)
-                            atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb +
+                            atomicAdd(&b.sub_dup[sub_key(b.nsub, o.gu, o.gv) * nb +
                                                  bin_index(g, plane, tv, tu)], 1u);
             }
         }
@@ -478,7 +464,7 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
         S fu, fv;
         BatchPoint bp;
         const int st = batch_point<UP2, WP2, S>(g, t, s_m0, m, o, fu, fv, bp);
-        const unsigned psub = st == 0 ? sub_key(g, b.nsub, o.gu, o.gv, o.tup, o.tvp) : 0u;
+        const unsigned psub = st == 0 ? sub_key(b.nsub, o.gu, o.gv) : 0u;
         for (int p = 0; p < t.pols; p++) {
             const int plane = (bp.c * t.pols + p) * g.wplanes + o.gw;
             const unsigned prim = (st == 0) ? psub * nb + bin_index(g, plane, o.tvp, o.tup) : kFull;
@@ -503,7 +489,7 @@ k_bin_scatter_batch(GeomParams g, ChanTable t, BinBuffers b, RecBuffers r)
                     const bool primary = tv == o.tvp && tu == o.tup;
                     const unsigned pos =
                         primary ? ppos
-                                : atomicAdd(&b.sub_dup[sub_key(g, b.nsub, o.gu, o.gv, tu, tv) * nb +
+                                : atomicAdd(&b.sub_dup[sub_key(b.nsub, o.gu, o.gv) * nb +
                                                        bin_index(g, plane, tv, tu)], 1u);
                     const int cu = o.gu - (tu << g.tile_shift);
                     const int cv = o.gv - (tv << g.tile_shift);

@@ -95,8 +95,8 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
 // loaded into shared memory with coalesced 16-byte loads and counting-sorted
 // by the Morton index of its (clamped) tile-relative cell, so the records of
 // one cell are consecutive: at 4096^2 x 32 planes and 50M measurements a
-// populated cell holds ~14 records, and the binning orders each bin's records
-// by blocks of T/4 x T/4 cells, so a stage covers a compact area at the bin's
+// populated cell holds ~14 records, and the binning keeps all records of a
+// cell in one sub-range of its bin, so a stage holds whole cells at the bin's
 // own density.  The sorted stage is cut into NS contiguous streams, one per
 // group of NT = 2K+1 lanes (RPW groups per warp).
 //

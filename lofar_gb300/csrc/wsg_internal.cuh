@@ -72,11 +72,11 @@ struct GeomParams {
 // no particular order), for kernels that skip empty bins.
 //
 // Counting uses nsub sub-counters per bin (nsub = kSub for plans, 1 for the
-// no-allocation entry point): a record uses the sub-counter of the 4x4 block
-// (in Morton order) that holds its tile-relative cell, clamped to the tile, in
-// both passes.  A bin's records are then grouped block by block, which keeps
-// each sorted stage of the FP32C gridder within a compact area, and the
-// atomics of a crowded bin are spread over nsub addresses.  After the scan,
+// no-allocation entry point): a record uses sub-counter (cu mod 4) + 4 (cv mod
+// 4) of its measurement's cell (cu, cv), in both passes.  The atomics of a
+// crowded bin are then spread over nsub addresses, and all records of one cell
+// stay in one sub-range, which keeps each cell's records together in the FP32C
+// gridder's sorted stages.  After the scan,
 // sub_prim[s][b] / sub_dup[s][b] hold the first record position of sub-range s
 // of bin b's primaries / duplicates and the scatter advances them as cursors.
 constexpr int kSub = 16;
