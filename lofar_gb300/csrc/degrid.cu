@@ -91,7 +91,8 @@ __device__ __forceinline__ void decode_bin_d(const GeomParams &g, unsigned bin, 
 }
 
 
-// Work item -> (bin, primaries [p0, p1)); the same items as the gridder.
+// Work item -> (bin, primaries [p0, p1)): the split items, then the occupied
+// bins that are not split (empty bins hold no primaries to degrid).
 __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, unsigned nsplit,
                                             unsigned &bin, unsigned &p0, unsigned &p1)
 {
@@ -101,8 +102,7 @@ __device__ __forceinline__ bool work_item_d(const BinBuffers &b, unsigned item, 
         bin = (unsigned)(e & 0xFFFFFFFFull);
         chunk = (unsigned)(e >> 32);
     } else {
-        bin = item - nsplit;
-        if (b.is_split[bin]) return false;
+        bin = b.work[item - nsplit];   // occupied bins that are not split
     }
     const unsigned nprim = b.nprim[bin];
     if (item < nsplit) {
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     const float2 *__restrict__ grid = reinterpret_cast<const float2 *>(a.grid);
     float2 *out = reinterpret_cast<float2 *>(a.out);
     const unsigned nsplit = a.b.ctr->nsplit_items;
-    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+    const unsigned nitems = nsplit + a.b.ctr->nwork;
     if (TMA && tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32d(&s_bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kThreadsD64, 2) k_degrid_f64(DegridArgs a)
     const double2 *__restrict__ fr_all = reinterpret_cast<const double2 *>(a.r.frac);
     double2 *out = reinterpret_cast<double2 *>(a.out);
     const unsigned nsplit = a.b.ctr->nsplit_items;
-    const unsigned nitems = nsplit + (unsigned)a.g.nbins;
+    const unsigned nitems = nsplit + a.b.ctr->nwork;
     double nt_u, t_v;
     taps64_consts<K>(lane, 0.5 / kRefPi, nt_u, t_v);
     const long long nt_uq = to_fixed(__double_as_longlong(nt_u), 62);
