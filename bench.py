@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shard", default="replicas", choices=["replicas", "planes"],
+                    help="N>1: replicas (every GPU images the whole workload, no exchange) or "
+                         "planes (one image; each GPU grids, transforms and w-corrects its "
+                         "w-plane range and the partial images are sum-reduced with NCCL)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "driver"],
                     help="c2: one 4096^2 x 32 image (default); c4: the channel x pol batch; "
                          "c5: one 8192^2 x 128 image, support 9, 400M visibilities; "
@@ -247,8 +251,10 @@ OUR_KERNELS_PER_STEP = {"bin": 6, "grid": 1, "fft_wcorrect": 2, "wcorrect_adj_ff
                         "degrid": 1}
 
 
-def run_plan_steps(plan, ins, image, out, steps, record_stages):
-    """`steps` forward+adjoint passes; returns (total_ms, {stage: [ms per step]})."""
+def run_plan_steps(plan, ins, image, out, steps, record_stages, reduce=None):
+    """`steps` forward+adjoint passes; returns (total_ms, {stage: [ms per step]}).
+    reduce: applied to the forward image before the adjoint (the plane-sharded
+    form's sum over ranks)."""
     import torch
     stream = torch.cuda.current_stream()
     per = {s: [] for s in STAGES}
@@ -268,6 +274,8 @@ def run_plan_steps(plan, ins, image, out, steps, record_stages):
         if evs:
             evs[2].record(stream)
         plan.fft_wcorrect(grid, out=image)
+        if reduce is not None:
+            reduce(image)
         if evs:
             evs[3].record(stream)
         plan.wcorrect_adjoint_fft(image, out=grid)
@@ -311,15 +319,25 @@ def bench_ours(args, rank, world):
     ins = (torch.as_tensor(obs.uu).cuda(), torch.as_tensor(obs.vv).cuda(),
            torch.as_tensor(obs.ww).cuda(), torch.as_tensor(obs.vis_real).cuda(),
            torch.as_tensor(obs.vis_img).cuda(), torch.as_tensor(obs.weight).cuda())
+    reduce = None
+    planes_mode = args.shard == "planes" and world > 1
+    if planes_mode:
+        # one image over all ranks: this rank's w-plane range and measurements;
+        # the partial images are summed by NCCL between forward and adjoint
+        from lofar_gb300.sharding import PlaneShard, plane_counts
+        shard = PlaneShard(P, 1.0 / P, plane_counts(obs.ww, 1.0 / P, P))
+        _, ins = shard.select(*ins)
+        reduce = shard._all_reduce
+    n_local = int(ins[0].numel())
 
     plan = Plan(nx, ny, P, args.support, precision="fp32c")
     plan.set_wcorrection(res, obs.wmin, obs.wmax)
-    plan.reserve(n)
+    plan.reserve(n_local)
     image = torch.empty((ny, nx), dtype=torch.complex64, device="cuda")
-    out = torch.empty(n, dtype=torch.complex64, device="cuda")
+    out = torch.empty(n_local, dtype=torch.complex64, device="cuda")
 
     # warm-up (also builds the w-screen table and the cuFFT plan)
-    run_plan_steps(plan, ins, image, out, args.warmup, False)
+    run_plan_steps(plan, ins, image, out, args.warmup, False, reduce)
     stats = plan.stats()
 
     if world > 1:
@@ -327,11 +345,16 @@ def bench_ours(args, rank, world):
     torch.cuda.synchronize()
     clocks = ClockSampler(dev)
     clocks.start()
-    total_ms, per = run_plan_steps(plan, ins, image, out, args.steps, True)
+    total_ms, per = run_plan_steps(plan, ins, image, out, args.steps, True, reduce)
     clk = clocks.stop()
     total_ms = max_over_ranks(total_ms, world)
     ms_per_step = total_ms / args.steps
-    value = whole_job_mvis(n, world, ms_per_step)
+    # replicas: every rank imaged all n visibilities; planes: one image of n
+    value = whole_job_mvis(n, 1 if planes_mode else world, ms_per_step)
+    if planes_mode:
+        return dict(rank=rank, n=n, res=res, wmin=obs.wmin, wmax=obs.wmax, gen_s=gen_s,
+                    ms_per_step=ms_per_step, value=value, per=per, stats=stats, clocks=clk,
+                    plan_bytes=plan.device_bytes(), planes=(shard.p0, shard.p1)), obs
 
     # forward image of the FP32C form (for the accuracy comparison)
     img32 = plan.image_forward(*ins).clone()
@@ -1057,16 +1080,18 @@ def main():
         "warmup": args.warmup,
         "ms_per_step": res["ms_per_step"],
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if "planes" in res else "weak",
         "vs_baseline": None,
         "dtype": "fp32c",
         "data": "synthetic (seeded; 62 stations in an 8 km disk, 8 h earth-rotation tracks, "
                 "20 point sources + noise)",
         "config": {"workload": f"w-stacking fwd+adjoint, {args.nx}x{args.nx} grid, {args.planes} "
-                               f"w-planes, support {args.support}, {n} visibilities per GPU",
-                   "precision": "FP32 complex grid, compensated tile accumulation, FP64-exact "
+                               f"w-planes, support {args.support}, {n} visibilities "
+                               + ("in one image over all GPUs" if "planes" in res else "per GPU"),
+                   "precision": "FP32 complex grid, int32 fixed-point tile sums, FP64-exact "
                                 "coordinates and phase argument",
-                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
+                   "parallelism": (f"planes{world}" if "planes" in res else f"replicas{world}"),
+                   "l2": "inputs larger than L2 (no flush)"},
         "roofline": {"bound": "hbm", "kernel": "gridding stage (bin_count+bin_scan+bin_scatter+grid)",
                      "achieved": g["gbs"], "peak": peak, "unit": "GB/s", "frac": g["frac"],
                      "peak_source": f"{peak_kind} hbm copy bandwidth",
@@ -1100,6 +1125,10 @@ def main():
                             statistics.median(f["per"]["fft_wcorrect"]))}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
+    if "planes" in res:
+        line["e2e"] = {"value": None, "unit": "Mvis/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0,
+                       "note": "not measured in the plane-sharded form (run N=1 for e2e)"}
     if not args.no_cpu and world >= 1:
         line["cpu_baseline"] = cpu_baseline(obs, res["res"], args, args.cpu_budget)
     print(json.dumps(line))
