@@ -58,8 +58,11 @@ def parse():
                     help="N>1: replicas (every GPU images the whole workload, no exchange) or "
                          "planes (one image; each GPU grids, transforms and w-corrects its "
                          "w-plane range and the partial images are sum-reduced with NCCL)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "driver"],
-                    help="c2: one 4096^2 x 32 image (default); c4: the channel x pol batch; "
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4", "c5", "driver"],
+                    help="c2: one 4096^2 x 32 image (default); c1: the reference's CPU "
+                         "configuration (512^2 x 8, 1M visibilities, 48 stations, 3 km, 4 h) "
+                         "with the reference CPU path timed in full beside it; "
+                         "c4: the channel x pol batch; "
                          "c5: one 8192^2 x 128 image, support 9, 400M visibilities; "
                          "driver: c2 as files through the reference's main()")
     ap.add_argument("--driver-dir", default=None,
@@ -80,10 +83,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     a = ap.parse_args()
     from lofar_gb300 import synth
-    cfg = synth.CONFIGS["c5" if a.workload == "c5" else "c2"]
+    cfg = synth.CONFIGS[a.workload if a.workload in ("c1", "c5") else "c2"]
     a.nvis = cfg["gen"]["n_vis"] if a.nvis is None else a.nvis
     a.nx = cfg["nx"] if a.nx is None else a.nx
     a.planes = cfg["planes"] if a.planes is None else a.planes
@@ -133,7 +135,7 @@ def whole_job_mvis(n_per_rank: int, world: int, ms_per_step: float) -> float:
 
 def workload(args, backend):
     from lofar_gb300 import synth
-    gen = dict(synth.CONFIGS["c2"]["gen"])
+    gen = dict(synth.CONFIGS["c1" if args.workload == "c1" else "c2"]["gen"])
     gen["n_vis"] = args.nvis
     t = time.time()
     obs = synth.observe(backend=backend, **gen)
@@ -464,84 +466,108 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def cpu_baseline(obs, res, args, budget_s):
-    """Time the oracle port per stage on samples, extrapolate to the full step."""
+def reference_step(obs, res, args, cores, grid):
+    """One whole fwd+adjoint step of the reference's CPU algorithm (the oracle
+    port, OpenMP on `cores` threads) on every measurement and every plane:
+    wstack (w-stacking.cu:222-311), the per-plane FFTW_BACKWARD x 1/(Nx*Ny)
+    (fourier_transform.c:25-59; scipy.fft stands in for FFTW, which is not
+    installed), phase_correction (phase_correction.cu:147-207), then the
+    adjoint chain (w-correction adjoint, forward FFT x 1/(Nx*Ny), degridding).
+    grid: a preallocated float64 [P][ny][nx][2] buffer.  Returns the seconds
+    of each stage."""
+    import scipy.fft as sfft
     from oracle import oracle as O
-    cores = cpu_cores()
     nx = ny = args.nx
     P = args.planes
-    n_full = obs.n
     kw = dict(num_w_planes=P, dx=1 / nx, dw=1 / P, w_support=args.support, nx=nx, ny=ny)
-    grid = np.zeros((P, ny, nx, 2), np.float64)
-    # calibrate on a small probe, then size the gridding sample to ~30% of the budget
-    probe = min(n_full, 200_000)
-    t = time.perf_counter()
-    O.wstack(obs.uu[:probe], obs.vv[:probe], obs.ww[:probe], obs.vis_real[:probe],
-             obs.vis_img[:probe], obs.weight[:probe], num_threads=cores, grid=grid, **kw)
-    rate = probe / max(time.perf_counter() - t, 1e-6)
-    m = int(min(n_full, max(probe, 0.3 * budget_s * rate)))
-    sel = slice(0, m)
-    grid[:] = 0.0
-    t = time.perf_counter()
-    O.wstack(obs.uu[sel], obs.vv[sel], obs.ww[sel], obs.vis_real[sel], obs.vis_img[sel],
-             obs.weight[sel], num_threads=cores, grid=grid, **kw)
-    t_grid = (time.perf_counter() - t) / m
-    t = time.perf_counter()
-    O.degrid(obs.uu[sel], obs.vv[sel], obs.ww[sel], grid, num_threads=cores, **kw)
-    t_degrid = (time.perf_counter() - t) / m
-    # FFT + w-correction on 2 planes, scaled per plane
-    k = 2
-    sub = grid[:k]
-    t = time.perf_counter()
-    gs = O.fft_planes(sub, workers=cores)
-    t_fft = (time.perf_counter() - t) / k
-    t = time.perf_counter()
-    O.fft_planes_adjoint(gs, workers=cores)
-    t_ffta = (time.perf_counter() - t) / k
-    t = time.perf_counter()
-    re, im = O.phase_correction(gs, nx=nx, ny=ny, num_w_planes=k, resolution=res, wmin=obs.wmin,
-                                wmax=obs.wmax, num_threads=cores)
-    t_ph = (time.perf_counter() - t) / k
-    t = time.perf_counter()
-    O.phase_adjoint(np.nan_to_num(re), np.nan_to_num(im), nx=nx, ny=ny, num_w_planes=k,
-                    resolution=res, wmin=obs.wmin, wmax=obs.wmax, num_threads=cores)
-    t_pha = (time.perf_counter() - t) / k
-    total = n_full * (t_grid + t_degrid) + P * (t_fft + t_ffta + t_ph + t_pha)
-    sample = (f"oracle port (OpenMP, {cores} threads): gridding+degridding timed on {m} of "
-              f"{n_full} measurements on the full {nx}x{ny}x{P} grid, FFT (scipy, FFTW "
-              f"substitute) and w-correction timed on {k} of {P} planes; per-unit times "
-              f"extrapolated to the full step")
-    return dict(value=n_full / total / 1e6, unit="Mvis/s", cores=cores, kind="port",
-                sample=sample, seconds_per_step_extrapolated=total,
-                per_unit=dict(grid_s_per_vis=t_grid, degrid_s_per_vis=t_degrid,
-                              fft_s_per_plane=t_fft, fft_adj_s_per_plane=t_ffta,
-                              wcorrect_s_per_plane=t_ph, wcorrect_adj_s_per_plane=t_pha))
+    wc = dict(nx=nx, ny=ny, num_w_planes=P, resolution=res, wmin=obs.wmin, wmax=obs.wmax,
+              num_threads=cores)
+    t = {}
+    c = time.perf_counter()
+
+    def lap(name):
+        nonlocal c
+        now = time.perf_counter()
+        t[name] = now - c
+        c = now
+
+    def fft_in_place(buf, forward):
+        z = buf.view(np.complex128)[..., 0]
+        f = sfft.fft2 if forward else sfft.ifft2
+        r = f(z, axes=(-2, -1), workers=cores, overwrite_x=True)
+        if forward:
+            r /= float(nx) * float(ny)
+        if not np.shares_memory(r, z):
+            z[...] = r
+
+    grid[...] = 0.0
+    O.wstack(obs.uu, obs.vv, obs.ww, obs.vis_real, obs.vis_img, obs.weight,
+             num_threads=cores, grid=grid, **kw)
+    lap("grid")
+    fft_in_place(grid, forward=False)
+    lap("fft")
+    re, im = O.phase_correction(grid, **wc)
+    lap("wcorrect")
+    # the adjoint of the image just formed (pixels where the reference's
+    # w-correction is undefined excluded)
+    planes = O.phase_adjoint(np.nan_to_num(re), np.nan_to_num(im), **wc)
+    lap("wcorrect_adj")
+    fft_in_place(planes, forward=True)
+    lap("fft_adj")
+    O.degrid(obs.uu, obs.vv, obs.ww, planes, num_threads=cores, **kw)
+    lap("degrid")
+    return t
+
+
+def cpu_baseline(obs, res, args, steps=1):
+    """The reference's CPU path timed over whole steps of the same workload on
+    this host's cores (no sampling, no extrapolation)."""
+    cores = cpu_cores()
+    grid = np.zeros((args.planes, args.nx, args.nx, 2), np.float64)   # touched once, reused
+    per = [reference_step(obs, res, args, cores, grid) for _ in range(steps)]
+    tot = [sum(p.values()) for p in per]
+    step_s = statistics.median(tot)
+    return dict(value=obs.n / step_s / 1e6, unit="Mvis/s", cores=cores, kind="port",
+                sample=(f"oracle port (OpenMP, {cores} threads; scipy.fft as the FFTW "
+                        f"substitute): {steps} whole fwd+adjoint step(s) over all {obs.n} "
+                        f"measurements and all {args.planes} planes of the "
+                        f"{args.nx}x{args.nx} grid"),
+                seconds_per_step=step_s,
+                stages_s={k: statistics.median(p[k] for p in per) for k in per[0]})
 
 
 def bench_reference(args, rank, world):
-    """--impl reference: the reference's CPU path (oracle port) on this host."""
+    """--impl reference: the reference's CPU path (oracle port) on this host,
+    whole steps of the same workload (one untimed warm-up step: the buffers and
+    the FFT plans are first touched there)."""
     if rank != 0:
         return None
     obs, res, _ = workload(args, "numpy")
     from oracle import build as obuild
     obuild.build_oracle()
-    per_step = max(5.0, 150.0 / max(1, args.steps + args.warmup))
-    for _ in range(args.warmup):
-        cpu_baseline(obs, res, args, per_step * 0.3)
-    vals, last = [], None
+    cores = cpu_cores()
+    grid = np.zeros((args.planes, args.nx, args.nx, 2), np.float64)
+    for _ in range(min(args.warmup, 1)):
+        reference_step(obs, res, args, cores, grid)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        last = cpu_baseline(obs, res, args, per_step)
-        vals.append(last["value"])
+    per = [reference_step(obs, res, args, cores, grid) for _ in range(args.steps)]
     wall = time.perf_counter() - t0
-    value = statistics.median(vals)
-    cb = dict(last)
-    cb["value"] = value
+    step_s = wall / max(args.steps, 1)
+    value = obs.n / step_s / 1e6
+    cb = dict(value=value, unit="Mvis/s", cores=cores, kind="port",
+              sample=(f"oracle port (OpenMP, {cores} threads; scipy.fft as the FFTW "
+                      f"substitute): {args.steps} timed whole fwd+adjoint steps over all "
+                      f"{obs.n} measurements and {args.planes} planes, after "
+                      f"{min(args.warmup, 1)} untimed"),
+              seconds_per_step=step_s,
+              stages_s={k: statistics.median(p[k] for p in per) for k in per[0]})
     return {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": obs.n / value / 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; 62 stations, 8 km, 8 h)",
+        "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": (f"synthetic (seeded; {obs.meta['n_stations']} stations, "
+                 f"{obs.meta['diameter_m'] / 1000:g} km, {obs.meta['hours']:g} h)"),
         "config": {"workload": f"w-stacking fwd+adjoint, {args.nx}x{args.nx} grid, {args.planes} "
                                f"w-planes, support {args.support}, {obs.n} visibilities",
                    "parallelism": f"replicas{args.gpus}", "l2": "inputs larger than L2"},
@@ -1083,8 +1109,9 @@ def main():
         "scaling": "strong" if "planes" in res else "weak",
         "vs_baseline": None,
         "dtype": "fp32c",
-        "data": "synthetic (seeded; 62 stations in an 8 km disk, 8 h earth-rotation tracks, "
-                "20 point sources + noise)",
+        "data": (f"synthetic (seeded; {obs.meta['n_stations']} stations in a "
+                 f"{obs.meta['diameter_m'] / 1000:g} km disk, {obs.meta['hours']:g} h earth-rotation "
+                 "tracks, 20 point sources + noise)"),
         "config": {"workload": f"w-stacking fwd+adjoint, {args.nx}x{args.nx} grid, {args.planes} "
                                f"w-planes, support {args.support}, {n} visibilities "
                                + ("in one image over all GPUs" if "planes" in res else "per GPU"),
@@ -1130,7 +1157,8 @@ def main():
                        "d2h_bytes_per_step": 0,
                        "note": "not measured in the plane-sharded form (run N=1 for e2e)"}
     if not args.no_cpu and world >= 1:
-        line["cpu_baseline"] = cpu_baseline(obs, res["res"], args, args.cpu_budget)
+        line["cpu_baseline"] = cpu_baseline(obs, res["res"], args,
+                                            steps=3 if args.workload == "c1" else 1)
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
