@@ -332,8 +332,12 @@ def bench_ours(args, rank, world):
         reduce = shard._all_reduce
     n_local = int(ins[0].numel())
 
+    # the synthetic measurements are [dump][baseline], as the reference's
+    # measurement sets are (meta.txt's `baselines`): the binning walks tracks
+    rows = 0 if planes_mode else obs.meta.get("n_baselines", 0)
     plan = Plan(nx, ny, P, args.support, precision="fp32c")
     plan.set_wcorrection(res, obs.wmin, obs.wmax)
+    plan.set_layout(rows)
     plan.reserve(n_local)
     image = torch.empty((ny, nx), dtype=torch.complex64, device="cuda")
     out = torch.empty(n_local, dtype=torch.complex64, device="cuda")
@@ -421,6 +425,7 @@ def bench_ours(args, rank, world):
         hout = torch.empty(n, dtype=torch.complex64).pin_memory()
         pe = Plan(nx, ny, P, args.support, precision="fp32c")
         pe.set_wcorrection(res, obs.wmin, obs.wmax)
+        pe.set_layout(rows)
         args_h = [pin[k] for k in ("uu", "vv", "ww", "vis_real", "vis_img", "weight")]
         pe.image_forward_host(*args_h, himg)
         pe.image_adjoint_host(himg, hout)

@@ -150,6 +150,14 @@ WSG_API int wsg_plan_set_stream(wsg_plan *plan, void *stream);
  * per work item of a bin cut into several; >= 512) -- 0 keeps the current
  * value (ctas 0 = automatic). */
 WSG_API int wsg_plan_set_tuning(wsg_plan *plan, int tile, int ctas, int chunk);
+/* Layout of the measurements: [dump][baseline] order with rows_per_dump rows
+ * per dump, as the reference's measurement sets are written (meta.txt's
+ * `baselines`, init.c:293).  An FP32C plan's binning then walks each
+ * baseline's consecutive dumps together, so records that share a bin merge
+ * their cursor atomics and are written contiguously.  A speed hint only: the
+ * grid does not depend on it (a wrong count only changes the speed); FP64
+ * plans keep the index-order walk; 0 (the default) walks in index order. */
+WSG_API int wsg_plan_set_layout(wsg_plan *plan, long rows_per_dump);
 /* Reserves device memory for up to max_points measurements so that later
  * calls allocate nothing (required before CUDA-graph capture). */
 WSG_API int wsg_plan_reserve(wsg_plan *plan, long max_points);

@@ -124,6 +124,7 @@ SIGNATURES = {
     "wsg_bin": (_I, [_P, _L, _L, _L, _P, _P, _P, _P, _P, _P]),
     "wsg_grid": (_I, [_P, _P]),
     "wsg_grid_occupied": (_I, [_P, _P]),
+    "wsg_plan_set_layout": (_I, [_P, _L]),
     "wsg_fft": (_I, [_P, _P, _I]),
     "wsg_wcorrect": (_I, [_P, _P, _P, _D]),
     "wsg_wcorrect_adjoint": (_I, [_P, _P, _P, _D]),

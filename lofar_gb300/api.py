@@ -139,6 +139,12 @@ class Plan:
     def set_tuning(self, tile: int = 0, ctas: int = 0, chunk: int = 0):
         check(self.lib.wsg_plan_set_tuning(self._h, int(tile), int(ctas), int(chunk)))
 
+    def set_layout(self, rows_per_dump: int):
+        """Measurements come as [dump][baseline] with rows_per_dump rows per
+        dump (the reference's measurement sets): a speed hint for the binning
+        of FP32C plans; 0 = unknown."""
+        check(self.lib.wsg_plan_set_layout(self._h, int(rows_per_dump)))
+
     def reserve(self, max_points: int):
         self._sync_stream()
         check(self.lib.wsg_plan_reserve(self._h, int(max_points)))

@@ -119,6 +119,21 @@ __device__ __forceinline__ long long tile_m(long long q, int i)
 // tile block (d: du = d & 1, dv = d >> 1 from (tu0, tv0)): indices into the
 // counter array sub_prim, which sub_dup follows (primaries, then duplicates);
 // kFull where the window has no tile.  dp: the primary's d.
+// Sub-range by position (walks along tracks): the 4x4 block (T/4 cells
+// square, Morton order) of the measurement's clamped cell in its primary
+// tile.  A track stays in one block for many dumps, so the records of a
+// baseline's consecutive dumps share counters; each cell still falls in one
+// sub-range.
+__device__ __forceinline__ unsigned block_key(const GeomParams &g, unsigned nsub, const MGeom &o)
+{
+    if (nsub < 16u) return 0u;
+    const int bs = g.tile_shift - 2;
+    const unsigned bx = (unsigned)(min(max(o.gu, 0), g.nx - 1) - (o.tup << g.tile_shift)) >> bs;
+    const unsigned by = (unsigned)(min(max(o.gv, 0), g.ny - 1) - (o.tvp << g.tile_shift)) >> bs;
+    return (bx & 1u) | ((by & 1u) << 1) | ((bx & 2u) << 1) | ((by & 2u) << 2);
+}
+
+template <bool SPATIAL>
 __device__ __forceinline__ void rec_keys(const GeomParams &g, const BinBuffers &b, const MGeom &o,
                                          int st, unsigned nb, unsigned key[4], int &dp)
 {
@@ -127,8 +142,9 @@ __device__ __forceinline__ void rec_keys(const GeomParams &g, const BinBuffers &
         key[0] = key[1] = key[2] = key[3] = kFull;
         return;
     }
+    const unsigned sub = SPATIAL ? block_key(g, b.nsub, o) : sub_key(b.nsub, o.gu, o.gv);
     const unsigned b0 = ((unsigned)o.gw * (unsigned)g.ntv + (unsigned)o.tv0) * (unsigned)g.ntu +
-                        (unsigned)o.tu0 + sub_key(b.nsub, o.gu, o.gv) * nb;
+                        (unsigned)o.tu0 + sub * nb;
     const bool two_u = o.tu1 > o.tu0, two_v = o.tv1 > o.tv0;
     dp = (o.tup - o.tu0) | ((o.tvp - o.tv0) << 1);
     const unsigned dupbase = b.nsub * nb;
@@ -190,7 +206,7 @@ k_bin_count(GeomParams g, const double *__restrict__ uu, const double *__restric
             ndw += st == 2;
             unsigned key[4];
             int dp;
-            rec_keys(g, b, o, st, nb, key, dp);
+            rec_keys<false>(g, b, o, st, nb, key, dp);
             unsigned kp = kFull;
 #pragma unroll
             for (int d = 0; d < 4; d++) kp = d == dp ? key[d] : kp;
@@ -289,7 +305,7 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
             MGeom o;
             const int st = m < n ? measure_cells<UP2, WP2>(g, x[i], y[i], z[i], o) : 3;
             unsigned key[4];
-            rec_keys(g, b, o, st, nb, key, dpi[i]);
+            rec_keys<false>(g, b, o, st, nb, key, dpi[i]);
             unsigned kp = kFull;
 #pragma unroll
             for (int d = 0; d < 4; d++) kp = d == dpi[i] ? key[d] : kp;
@@ -353,6 +369,176 @@ k_bin_scatter(GeomParams g, const double *__restrict__ uu, const double *__restr
                 if (tu == o.tup && tv == o.tvp) r.idx[p] = (unsigned)m;
             }
         }
+    }
+}
+
+// ---- the [dump][baseline] walk --------------------------------------------
+//
+// The reference's measurement sets hold their rows dump by dump, `baselines`
+// rows each (meta.txt, init.c:293).  Told that count (rows = B), the two
+// passes walk tiles of 32 dumps x 8 baselines (256 measurements, one a
+// thread): each dump's 8 baselines are loaded as one contiguous segment and
+// transposed through shared memory, so that warp w holds baseline 8 bb + w at
+// 32 consecutive dumps, lane l dump 32 tb + l.  A baseline's track moves by a
+// fraction of a cell per dump, so consecutive lanes mostly share the counters
+// of their records (the sub-ranges are then 4x4 blocks of the tile, which a
+// track crosses rarely): one cursor atomic per run of equal counters, for the
+// duplicates too, and a run's records land in consecutive positions, written
+// by consecutive lanes.
+struct RowsWalk {
+    long long n, rows;
+    unsigned nbb;       // blocks of 8 baselines
+    long long tiles;
+};
+
+__device__ __forceinline__ long long rows_m(const RowsWalk &w, unsigned tb, unsigned bb, int t,
+                                            int j)
+{
+    const long long bl = (long long)bb * 8 + j;
+    const long long m = ((long long)tb * 32 + t) * w.rows + bl;
+    return (bl < w.rows && m < w.n) ? m : -1;
+}
+
+template <bool UP2, bool WP2>
+__global__ void __launch_bounds__(256)
+k_bin_count_rows(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
+                 const double *__restrict__ ww, RowsWalk wk, BinBuffers b)
+{
+    __shared__ double su[32][9], sv[32][9], sw[32][9];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned nb = (unsigned)g.nbins;
+    for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
+        const unsigned tb = (unsigned)(q / wk.nbb), bb = (unsigned)(q - (long long)tb * wk.nbb);
+        {
+            const int t = tid >> 3, j = tid & 7;
+            const long long m = rows_m(wk, tb, bb, t, j);
+            su[t][j] = m >= 0 ? __ldcs(uu + m) : 0.0;
+            sv[t][j] = m >= 0 ? __ldcs(vv + m) : 0.0;
+            sw[t][j] = m >= 0 ? __ldcs(ww + m) : 0.0;
+        }
+        __syncthreads();
+        const long long m = rows_m(wk, tb, bb, lane, warp);
+        MGeom o;
+        const int st = m >= 0 ? measure_cells<UP2, WP2>(g, su[lane][warp], sv[lane][warp],
+                                                         sw[lane][warp], o)
+                              : 3;
+        unsigned key[4];
+        int dp;
+        rec_keys<true>(g, b, o, st, nb, key, dp);
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+            if (!__any_sync(kFull, key[d] != kFull)) continue;
+            int lead;
+            unsigned cnt, rank;
+            warp_runs(key[d], lane, lead, cnt, rank);
+            if (key[d] != kFull && lane == lead) atomicAdd(&b.sub_prim[key[d]], cnt);
+        }
+        int ndp = st == 1, ndw = st == 2;
+        for (int d = 16; d >= 1; d >>= 1) {
+            ndp += __shfl_xor_sync(kFull, ndp, d);
+            ndw += __shfl_xor_sync(kFull, ndw, d);
+        }
+        if (lane == 0) {
+            if (ndp) atomicAdd(&b.ctr->dropped_plane, (unsigned long long)ndp);
+            if (ndw) atomicAdd(&b.ctr->dropped_window, (unsigned long long)ndw);
+        }
+        __syncthreads();   // the tile's inputs are read before the next tile's land
+    }
+}
+
+template <bool UP2, bool WP2, int PREC>
+__global__ void __launch_bounds__(256)
+k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
+                   const double *__restrict__ ww, const float *__restrict__ vr,
+                   const float *__restrict__ vi, const float *__restrict__ wt, RowsWalk wk,
+                   long long nf, long long np, BinBuffers b, RecBuffers r)
+{
+    using S = typename std::conditional<PREC == WSG_FP64, double, float>::type;
+    __shared__ double su[32][9], sv[32][9], sw[32][9];
+    __shared__ float sr[32][9], si[32][9], st_[32][9];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned nb = (unsigned)g.nbins;
+    const bool single = nf == 1 && np == 1;
+    for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
+        const unsigned tb = (unsigned)(q / wk.nbb), bb = (unsigned)(q - (long long)tb * wk.nbb);
+        {
+            const int t = tid >> 3, j = tid & 7;
+            const long long m = rows_m(wk, tb, bb, t, j);
+            su[t][j] = m >= 0 ? __ldcs(uu + m) : 0.0;
+            sv[t][j] = m >= 0 ? __ldcs(vv + m) : 0.0;
+            sw[t][j] = m >= 0 ? __ldcs(ww + m) : 0.0;
+            sr[t][j] = (single && m >= 0) ? __ldcs(vr + m) : 0.0f;
+            si[t][j] = (single && m >= 0) ? __ldcs(vi + m) : 0.0f;
+            st_[t][j] = (single && m >= 0) ? __ldcs(wt + m) : 0.0f;
+        }
+        __syncthreads();
+        const long long m = rows_m(wk, tb, bb, lane, warp);
+        const double x = su[lane][warp], y = sv[lane][warp], z = sw[lane][warp];
+        MGeom o;
+        const int st = m >= 0 ? measure_cells<UP2, WP2>(g, x, y, z, o) : 3;
+        unsigned key[4];
+        int dp;
+        rec_keys<true>(g, b, o, st, nb, key, dp);
+        // every cursor atomic of the tile is issued before the first result
+        // is used: one per run of equal counters
+        unsigned got[4], lr[4];
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+            got[d] = 0u;
+            lr[d] = 0u;
+            if (!__any_sync(kFull, key[d] != kFull)) continue;
+            int lead;
+            unsigned cnt, rank;
+            warp_runs(key[d], lane, lead, cnt, rank);
+            if (key[d] != kFull && lane == lead) got[d] = atomicAdd(&b.sub_prim[key[d]], cnt);
+            lr[d] = ((unsigned)lead << 8) | rank;
+        }
+        unsigned pos[4];
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+            const unsigned base = __shfl_sync(kFull, got[d], (int)(lr[d] >> 8));
+            pos[d] = key[d] != kFull ? base + (lr[d] & 0xFFu) : kFull;
+        }
+        if (st == 0) {
+            S fu = 0, fv = 0;
+            unsigned qu = 0u, qv = 0u;
+            if (PREC == WSG_FP64) {
+                measure<UP2, WP2, S>(g, x, y, z, o, fu, fv);
+            } else {
+                bool ok;
+                coord_cell_q24<UP2>(x, g.ku, g.dx, qu, ok);
+                coord_cell_q24<UP2>(y, g.ku, g.dx, qv, ok);
+            }
+            S re, im;
+            if (single) {
+                // the fold of w-stacking.cu:98-112 with one entry
+                const float a = sr[lane][warp], w = st_[lane][warp];
+                re = isnan(a) ? (S)0 : (S)(w * a);
+                im = isnan(a) ? (S)0 : (S)(w * si[lane][warp]);
+            } else {
+                fold_value<S>(vr, vi, wt, m, nf, np, re, im);
+            }
+#pragma unroll
+            for (int d = 0; d < 4; d++) {
+                const unsigned p = pos[d];
+                if (p == kFull) continue;
+                const int tu = o.tu0 + (d & 1), tv = o.tv0 + (d >> 1);
+                const int cu = o.gu - (tu << g.tile_shift);
+                const int cv = o.gv - (tv << g.tile_shift);
+                if (PREC == WSG_FP64) {
+                    r.cell[p] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
+                    reinterpret_cast<double2 *>(r.frac)[p] = make_double2(fu, fv);
+                    reinterpret_cast<double2 *>(r.val)[p] = make_double2(re, im);
+                } else {
+                    r.rec16[p] = make_uint4(((unsigned)(cu + 64) << 24) | qu,
+                                            ((unsigned)(cv + 64) << 24) | qv,
+                                            __float_as_uint((float)re), __float_as_uint((float)im));
+                }
+                // only the degridder reads idx, and only of primaries
+                if (d == dp) r.idx[p] = (unsigned)m;
+            }
+        }
+        __syncthreads();   // the tile's inputs are read before the next tile's land
     }
 }
 
@@ -706,6 +892,14 @@ __global__ void __launch_bounds__(kScanThreads) k_bin_scan_c(long long nbins, Bi
     }
 }
 
+RowsWalk make_rows_walk(long long n, long long rows)
+{
+    const long long dumps = (n + rows - 1) / rows;
+    RowsWalk w{n, rows, (unsigned)((rows + 7) / 8), 0};
+    w.tiles = (dumps + 31) / 32 * (long long)w.nbb;
+    return w;
+}
+
 int tile_grid(long long tiles)
 {
     return (int)max(1ll, min(tiles, (long long)num_sms() * 8));
@@ -719,6 +913,15 @@ cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double
                              const double *ww, long long n, const BinBuffers &b, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    if (g.rows > 1 && g.rows < n) {
+        const RowsWalk w = make_rows_walk(n, g.rows);
+        const int blocks = tile_grid(w.tiles);
+        if (g.u_pow2 && g.w_pow2) k_bin_count_rows<true, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, w, b);
+        else if (g.u_pow2) k_bin_count_rows<true, false><<<blocks, 256, 0, s>>>(g, uu, vv, ww, w, b);
+        else if (g.w_pow2) k_bin_count_rows<false, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, w, b);
+        else k_bin_count_rows<false, false><<<blocks, 256, 0, s>>>(g, uu, vv, ww, w, b);
+        return cudaGetLastError();
+    }
     const long long tiles = (n + 256 * kItemsCount - 1) / (256 * kItemsCount);
     const int blocks = tile_grid(tiles);
     if (g.u_pow2 && g.w_pow2) k_bin_count<true, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, n, tiles, b);
@@ -743,6 +946,19 @@ static void scatter_dispatch(const GeomParams &g, const double *uu, const double
                              const float *wt, long long n, long long nf, long long np,
                              const BinBuffers &b, const RecBuffers &r, cudaStream_t s)
 {
+    if (g.rows > 1 && g.rows < n) {
+        const RowsWalk w = make_rows_walk(n, g.rows);
+        const int blocks = tile_grid(w.tiles);
+        if (g.u_pow2 && g.w_pow2)
+            k_bin_scatter_rows<true, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+        else if (g.u_pow2)
+            k_bin_scatter_rows<true, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+        else if (g.w_pow2)
+            k_bin_scatter_rows<false, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+        else
+            k_bin_scatter_rows<false, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+        return;
+    }
     const long long tiles = (n + 256 * kItemsScatter - 1) / (256 * kItemsScatter);
     const int blocks = tile_grid(tiles);
     if (g.u_pow2 && g.w_pow2)

@@ -133,6 +133,9 @@ int wsg::plan_configure(wsg_plan *p)
     g.nbins = p->cube_planes() * g.ntv * g.ntu;
     g.dx = p->dx;
     g.dw = p->dw;
+    // the [dump][baseline] walk serves FP32C plans; the FP64 gridder's
+    // record groups would collide on the shared cells of one track's records
+    g.rows = p->prec == WSG_FP32C ? p->rows : 0;
     int k = 0;
     g.u_pow2 = is_pow2_recip(p->dx, k) ? 1 : 0;
     g.ku = g.u_pow2 ? k : 0;
@@ -371,6 +374,16 @@ int wsg_plan_set_tuning(wsg_plan *p, int tile, int ctas, int chunk)
     p->ctas_user = ctas;
     if (tile) p->tile = tile;
     return plan_configure(p);
+}
+
+int wsg_plan_set_layout(wsg_plan *p, long rows_per_dump)
+{
+    clear_error();
+    if (!p) return set_error(WSG_ERR_ARG, "plan is NULL");
+    if (rows_per_dump < 0) return set_error(WSG_ERR_ARG, "negative rows per dump");
+    p->rows = rows_per_dump;
+    p->geom.rows = p->prec == WSG_FP32C ? rows_per_dump : 0;
+    return WSG_OK;
 }
 
 int wsg_plan_reserve(wsg_plan *p, long max_points)

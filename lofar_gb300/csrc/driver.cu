@@ -119,6 +119,9 @@ int prepare_device(DeviceSide &d, const wsg_params &prm, const wsg_metadata &met
                             1.0 / (double)planes, o.precision, stream));
     d.plan.reset(raw);
     WSG_TRY(wsg_plan_set_wcorrection(raw, resolution, meta.wmin, meta.wmax));
+    // the reference's measurement sets are written dump by dump, `baselines`
+    // rows each; one rank reads them from row 0
+    if (meta.baselines > 1) WSG_TRY(wsg_plan_set_layout(raw, meta.baselines));
     WSG_TRY(wsg_plan_reserve(raw, meta.Nmeasures));
     const size_t b_uvw = sizeof(double) * meta.Nmeasures, b_wt = sizeof(float) * meta.Nweights,
                  b_vis = sizeof(float) * meta.Nvis;

@@ -83,6 +83,7 @@ struct wsg_plan {
     double dx, dw;
     cudaStream_t stream = nullptr;
     int tile = 64, ctas_grid = 0, ctas_degrid = 0, split = wsg::kDefaultSplit, ctas_user = 0;
+    long long rows = 0;   // measurements per dump of the inputs' layout (0 = unknown)
     wsg::GeomParams geom{};
 
     wsg::DevBuf grid;                          // resident [jobs*P][Ny][Nx] complex

@@ -63,6 +63,7 @@ struct GeomParams {
     int ku, kw;
     double dx, dw;
     long long nbins;
+    long long rows;       // measurements per dump of a [dump][baseline] layout, 0 = unknown
 };
 
 // Work decomposition.  A bin with more than `split` records is cut into

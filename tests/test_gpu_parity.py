@@ -265,3 +265,27 @@ def test_fp32c_grid_is_deterministic_without_split_bins(gpu):
         grids.append(p.grid().cpu())
         p.close()
     assert torch.equal(torch.view_as_real(grids[0]), torch.view_as_real(grids[1]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_layout_hint_changes_only_the_walk(medium, precision):
+    """The [dump][baseline] walk of the binning (wsg_plan_set_layout) with the
+    observation's true baseline count, and with a wrong one, grids what the
+    index-order walk grids: FP64 (which keeps the index-order walk) against the
+    oracle at 1e-12, FP32C at the FP32C grid tolerances (split bins' chunks
+    hold other records, so their per-item scales and roundings differ)."""
+    import torch
+    o = medium["obs"]
+    for rows in (0, o.meta["n_baselines"], 1000, 7):
+        p = _plan(medium, precision)
+        p.set_layout(rows)
+        p.bin(o.uu, o.vv, o.ww, o.vis_real, o.vis_img, o.weight)
+        g = torch.view_as_real(p.grid()).double().cpu().numpy()
+        st = p.stats()
+        assert st["points_in"] == o.n and st["dropped_plane"] == 0
+        p.close()
+        if precision == "fp64":
+            assert _nrm_max(g, medium["grid"]) <= 1e-12, rows
+        else:
+            assert _nrm_rms(g, medium["grid"]) <= 1e-6, rows
+            assert _nrm_max(g, medium["grid"]) <= 1e-5, rows
