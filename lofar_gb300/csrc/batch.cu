@@ -138,6 +138,7 @@ int batch_forward(wsg_batch *B, void *images, int use_graph)
         }
     }
     p->n_binned = (long long)B->nvis;
+    p->walked = false;
     p->masks_valid = true;
     B->forwarded = true;
     return WSG_OK;

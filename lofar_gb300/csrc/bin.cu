@@ -399,6 +399,22 @@ __device__ __forceinline__ long long rows_m(const RowsWalk &w, unsigned tb, unsi
     return (bl < w.rows && m < w.n) ? m : -1;
 }
 
+// Loads the coordinates of dump t, baseline j of walk tile q (zeros outside
+// the measurements); returns the measurement's index, or -1.
+__device__ __forceinline__ long long rows_load3(const RowsWalk &w, long long q, int t, int j,
+                                               const double *__restrict__ uu,
+                                               const double *__restrict__ vv,
+                                               const double *__restrict__ ww, double &u, double &v,
+                                               double &x)
+{
+    const unsigned tb = (unsigned)(q / w.nbb), bb = (unsigned)(q - (long long)tb * w.nbb);
+    const long long m = rows_m(w, tb, bb, t, j);
+    u = m >= 0 ? __ldcs(uu + m) : 0.0;
+    v = m >= 0 ? __ldcs(vv + m) : 0.0;
+    x = m >= 0 ? __ldcs(ww + m) : 0.0;
+    return m;
+}
+
 template <bool UP2, bool WP2>
 __global__ void __launch_bounds__(256)
 k_bin_count_rows(GeomParams g, const double *__restrict__ uu, const double *__restrict__ vv,
@@ -406,17 +422,19 @@ k_bin_count_rows(GeomParams g, const double *__restrict__ uu, const double *__re
 {
     __shared__ double su[32][9], sv[32][9], sw[32][9];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lt = tid >> 3, lj = tid & 7;   // this thread's load: dump lt, baseline lj
     const unsigned nb = (unsigned)g.nbins;
+    // the next tile's coordinates are loaded into registers while the
+    // current tile is processed
+    double pu = 0.0, pv = 0.0, pw = 0.0;
+    if ((long long)blockIdx.x < wk.tiles) rows_load3(wk, blockIdx.x, lt, lj, uu, vv, ww, pu, pv, pw);
     for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
         const unsigned tb = (unsigned)(q / wk.nbb), bb = (unsigned)(q - (long long)tb * wk.nbb);
-        {
-            const int t = tid >> 3, j = tid & 7;
-            const long long m = rows_m(wk, tb, bb, t, j);
-            su[t][j] = m >= 0 ? __ldcs(uu + m) : 0.0;
-            sv[t][j] = m >= 0 ? __ldcs(vv + m) : 0.0;
-            sw[t][j] = m >= 0 ? __ldcs(ww + m) : 0.0;
-        }
+        su[lt][lj] = pu;
+        sv[lt][lj] = pv;
+        sw[lt][lj] = pw;
         __syncthreads();
+        if (q + gridDim.x < wk.tiles) rows_load3(wk, q + gridDim.x, lt, lj, uu, vv, ww, pu, pv, pw);
         const long long m = rows_m(wk, tb, bb, lane, warp);
         MGeom o;
         const int st = m >= 0 ? measure_cells<UP2, WP2>(g, su[lane][warp], sv[lane][warp],
@@ -459,19 +477,28 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned nb = (unsigned)g.nbins;
     const bool single = nf == 1 && np == 1;
+    const int lt = tid >> 3, lj = tid & 7;   // this thread's load: dump lt, baseline lj
+    // the next tile's inputs are loaded into registers while the current tile
+    // is processed
+    double pu = 0.0, pv = 0.0, pw = 0.0;
+    float pr = 0.0f, pi = 0.0f, pt = 0.0f;
+    auto load = [&](long long qq) {
+        const long long mm = rows_load3(wk, qq, lt, lj, uu, vv, ww, pu, pv, pw);
+        pr = (single && mm >= 0) ? __ldcs(vr + mm) : 0.0f;
+        pi = (single && mm >= 0) ? __ldcs(vi + mm) : 0.0f;
+        pt = (single && mm >= 0) ? __ldcs(wt + mm) : 0.0f;
+    };
+    if ((long long)blockIdx.x < wk.tiles) load(blockIdx.x);
     for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
         const unsigned tb = (unsigned)(q / wk.nbb), bb = (unsigned)(q - (long long)tb * wk.nbb);
-        {
-            const int t = tid >> 3, j = tid & 7;
-            const long long m = rows_m(wk, tb, bb, t, j);
-            su[t][j] = m >= 0 ? __ldcs(uu + m) : 0.0;
-            sv[t][j] = m >= 0 ? __ldcs(vv + m) : 0.0;
-            sw[t][j] = m >= 0 ? __ldcs(ww + m) : 0.0;
-            sr[t][j] = (single && m >= 0) ? __ldcs(vr + m) : 0.0f;
-            si[t][j] = (single && m >= 0) ? __ldcs(vi + m) : 0.0f;
-            st_[t][j] = (single && m >= 0) ? __ldcs(wt + m) : 0.0f;
-        }
+        su[lt][lj] = pu;
+        sv[lt][lj] = pv;
+        sw[lt][lj] = pw;
+        sr[lt][lj] = pr;
+        si[lt][lj] = pi;
+        st_[lt][lj] = pt;
         __syncthreads();
+        if (q + gridDim.x < wk.tiles) load(q + gridDim.x);
         const long long m = rows_m(wk, tb, bb, lane, warp);
         const double x = su[lane][warp], y = sv[lane][warp], z = sw[lane][warp];
         MGeom o;
@@ -913,7 +940,7 @@ cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double
                              const double *ww, long long n, const BinBuffers &b, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    if (g.rows > 1 && g.rows < n) {
+    if (rows_walk(g, n)) {
         const RowsWalk w = make_rows_walk(n, g.rows);
         const int blocks = tile_grid(w.tiles);
         if (g.u_pow2 && g.w_pow2) k_bin_count_rows<true, true><<<blocks, 256, 0, s>>>(g, uu, vv, ww, w, b);
@@ -946,7 +973,7 @@ static void scatter_dispatch(const GeomParams &g, const double *uu, const double
                              const float *wt, long long n, long long nf, long long np,
                              const BinBuffers &b, const RecBuffers &r, cudaStream_t s)
 {
-    if (g.rows > 1 && g.rows < n) {
+    if (rows_walk(g, n)) {
         const RowsWalk w = make_rows_walk(n, g.rows);
         const int blocks = tile_grid(w.tiles);
         if (g.u_pow2 && g.w_pow2)

@@ -475,6 +475,7 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
     WSG_CUDA(launch_bin_scatter(p->geom, p->prec, uu, vv, ww, vr, vi, wt, n, nf, np, b,
                                 p->recbufs(), p->stream));
     p->n_binned = n;
+    p->walked = rows_walk(p->geom, n);
     return finish_binning(p);
 }
 
@@ -486,7 +487,7 @@ int wsg_grid(wsg_plan *p, void *grid)
     const BinBuffers b = p->binbufs();
     WSG_CUDA(cudaMemsetAsync(&b.ctr->work_grid, 0, sizeof(unsigned), p->stream));
     WSG_CUDA(launch_grid(p->geom, p->prec, b, p->recbufs(), grid, p->partials.p, p->ctas_grid,
-                         p->stream));
+                         p->stream, false, p->walked));
     return WSG_OK;
 }
 
@@ -498,7 +499,7 @@ int wsg_grid_occupied(wsg_plan *p, void *grid)
     const BinBuffers b = p->binbufs();
     WSG_CUDA(cudaMemsetAsync(&b.ctr->work_grid, 0, sizeof(unsigned), p->stream));
     WSG_CUDA(launch_grid(p->geom, p->prec, b, p->recbufs(), grid, p->partials.p, p->ctas_grid,
-                         p->stream, p->fused));
+                         p->stream, p->fused, p->walked));
     return WSG_OK;
 }
 

@@ -100,6 +100,13 @@ __device__ __forceinline__ bool work_item(const BinBuffers &b, unsigned item, un
 // own density.  The sorted stage is cut into NS contiguous streams, one per
 // group of NT = 2K+1 lanes (RPW groups per warp).
 //
+// Track order (SORTED = false): when the binning walked the measurements
+// baseline by baseline (the [dump][baseline] walk), a bin holds each
+// baseline's consecutive dumps in consecutive records, and a track crosses a
+// cell in ~10 dumps at 4096^2 (a sorted stage gathers ~14 records per cell).
+// Stages are then used as stored: no counting sort, two barriers per stage
+// instead of six.
+//
 // Lane k of a group owns window row k of its stream's records and keeps NT
 // register accumulators, one per window column.  While consecutive records
 // sit in the same cell their windows cover the same cells, so the taps keep
@@ -144,7 +151,7 @@ __device__ __forceinline__ unsigned cell_key(const uint4 &q)
     return spread6((unsigned)cu) | (spread6((unsigned)cv) << 1);
 }
 
-template <int T, int K>
+template <int T, int K, bool SORTED>
 __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
 {
     constexpr int kThreadsR = f32c_threads(K);
@@ -229,34 +236,23 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
         // from the item's largest value and record count (sums stay below
         // 2^31), so the bound is an upper bound, independent of the order of
         // the records.
-        for (int i = tid; i < NB * NB; i += kThreadsR) s_blk[i] = 0u;
-        float vmax = 0.0f;
-        for (unsigned i = r0 + tid; i < r1; i += kThreadsR) {
-            const uint4 q = __ldcg(rec + off + i);
-            vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(q.z)), fabsf(__uint_as_float(q.w))));
-        }
-        for (int d = 16; d >= 1; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xFFFFFFFFu, vmax, d));
-        if (lane == 0) s_vmax[warp] = vmax;
-        __syncthreads();
-        float tapmax = 0.0f;
-#pragma unroll
-        for (int i = 0; i < NW; i++) tapmax = fmaxf(tapmax, s_vmax[i]);
-        float bound = 0.0f;
-        if (tapmax > 0.0f) {
+        const unsigned n = r1 - r0;
+        // block-sum scale 2^sc: terms <= 2^(31-lb) for n < 2^lb records
+        auto sum_scale = [&](float tmax) {
             int ev;
-            frexpf(tapmax, &ev);                    // |Re V| + |Im V| < 2^(ev+1)
-            const int lb = 32 - __clz(r1 - r0);     // record count < 2^lb
-            const int sc = min(30 - lb - ev, 126);  // terms <= 2^(31-lb): sums < 2^31
-            const float up = ldexpf(1.0f, sc);
-            for (unsigned i = r0 + tid; i < r1; i += kThreadsR) {
-                const uint4 q = __ldcg(rec + off + i);
-                const int bx = ((int)(q.x >> 24) - 64 + H) >> BS;
-                const int by = ((int)(q.y >> 24) - 64 + H) >> BS;
-                const float v = fabsf(__uint_as_float(q.z)) + fabsf(__uint_as_float(q.w));
-                // v*up rounded up twice: the product toward +inf, then ceil
-                atomicAdd(&s_blk[by * NB + bx], (unsigned)ceilf(__fmul_ru(v, up)));
-            }
-            __syncthreads();
+            frexpf(tmax, &ev);                      // |Re V| + |Im V| < 2^(ev+1)
+            const int lb = 32 - __clz(n);           // record count < 2^lb
+            return min(30 - lb - ev, 126);
+        };
+        auto add_block = [&](const uint4 &q, float up) {
+            const int bx = ((int)(q.x >> 24) - 64 + H) >> BS;
+            const int by = ((int)(q.y >> 24) - 64 + H) >> BS;
+            const float v = fabsf(__uint_as_float(q.z)) + fabsf(__uint_as_float(q.w));
+            // v*up rounded up twice: the product toward +inf, then ceil
+            atomicAdd(&s_blk[by * NB + bx], (unsigned)ceilf(__fmul_ru(v, up)));
+        };
+        // largest 3x3-block sum, reduced over the warp into s_part[warp]
+        auto block_max = [&]() {
             unsigned long long bmax = 0ull;
             for (int i = tid; i < NB * NB; i += kThreadsR) {
                 const int by = i / NB, bx = i - (i / NB) * NB;
@@ -268,10 +264,130 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
             }
             for (int d = 16; d >= 1; d >>= 1) bmax = max(bmax, __shfl_xor_sync(0xFFFFFFFFu, bmax, d));
             if (lane == 0) s_part[warp] = __ull2float_ru(bmax);
-            __syncthreads();
+        };
+        auto warp_vmax = [&](float vmax) {
+            for (int d = 16; d >= 1; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xFFFFFFFFu, vmax, d));
+            if (lane == 0) s_vmax[warp] = vmax;
+        };
+        auto cta_max = [&](const float *s) {
+            float m = 0.0f;
 #pragma unroll
-            for (int i = 0; i < NW; i++) bound = fmaxf(bound, s_part[i]);
-            bound = ldexpf(bound, -sc);
+            for (int i = 0; i < NW; i++) m = fmaxf(m, s[i]);
+            return m;
+        };
+        // the staged records' bucket counts (two 16-bit counts per word)
+        auto count_keys = [&](const unsigned (&key)[RPT], unsigned cnt) {
+#pragma unroll
+            for (int t = 0; t < RPT; t++)
+                if (tid + t * kThreadsR < cnt)
+                    atomicAdd(&hist[key[t] >> 1], (key[t] & 1u) ? 0x10000u : 1u);
+        };
+        // exclusive scan of the bucket counts, buckets in key order (a cursor
+        // never exceeds cnt < 2^16): the warp scans, then (after a barrier)
+        // the CTA's prefix and the cursors
+        unsigned wv[KW], s_run = 0u, s_incl = 0u;
+        auto scan_warps = [&]() {
+            s_run = 0u;
+#pragma unroll
+            for (int t = 0; t < KW; t++) {
+                wv[t] = hist[tid * KW + t];
+                s_run += (wv[t] & 0xFFFFu) + (wv[t] >> 16);
+            }
+            s_incl = s_run;
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned y = __shfl_up_sync(0xFFFFFFFFu, s_incl, d);
+                if (lane >= d) s_incl += y;
+            }
+            if (lane == 31) s_wsum[warp] = s_incl;
+        };
+        auto scan_cursors = [&]() {
+            unsigned base = s_incl - s_run;
+            for (int i = 0; i < warp; i++) base += s_wsum[i];
+#pragma unroll
+            for (int t = 0; t < KW; t++) {
+                const unsigned lo = wv[t] & 0xFFFFu, hi = wv[t] >> 16;
+                hist[tid * KW + t] = base | ((base + lo) << 16);
+                base += lo + hi;
+            }
+        };
+        auto place = [&](const unsigned (&key)[RPT], unsigned cnt) {
+#pragma unroll
+            for (int t = 0; t < RPT; t++) {
+                const unsigned i = tid + t * kThreadsR;
+                if (i < cnt) {
+                    const unsigned old = atomicAdd(&hist[key[t] >> 1], (key[t] & 1u) ? 0x10000u : 1u);
+                    sidx[(key[t] & 1u) ? (old >> 16) : (old & 0xFFFFu)] = (unsigned short)i;
+                }
+            }
+        };
+
+        float tapmax = 0.0f, bound = 0.0f;
+        unsigned key[RPT];
+        const bool one_stage = n <= (unsigned)kStageR;
+        if (one_stage) {
+            // The whole item fits one stage: its records are read once, and
+            // the bound, the sort keys and the bucket counts all come from
+            // the staged copy (five barriers instead of ten; three in track
+            // order).
+            for (int i = tid; i < NB * NB; i += kThreadsR) s_blk[i] = 0u;
+            if (SORTED)
+                for (int i = tid; i < NKEY / 2; i += kThreadsR) hist[i] = 0u;
+            float vmax = 0.0f;
+#pragma unroll
+            for (int t = 0; t < RPT; t++) {
+                const unsigned i = tid + t * kThreadsR;
+                key[t] = 0u;
+                if (i < n) {
+                    const uint4 q = __ldcs(rec + off + r0 + i);
+                    stage[i] = q;
+                    if (SORTED) key[t] = cell_key<T>(q);
+                    vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(q.z)), fabsf(__uint_as_float(q.w))));
+                }
+            }
+            warp_vmax(vmax);
+            __syncthreads();
+            tapmax = cta_max(s_vmax);
+            if (SORTED) count_keys(key, n);
+            int sc = 0;
+            if (tapmax > 0.0f) {
+                sc = sum_scale(tapmax);
+                const float up = ldexpf(1.0f, sc);
+#pragma unroll
+                for (int t = 0; t < RPT; t++) {
+                    const unsigned i = tid + t * kThreadsR;
+                    if (i < n) add_block(stage[i], up);   // this thread's own records
+                }
+            }
+            __syncthreads();
+            if (SORTED) scan_warps();
+            if (tapmax > 0.0f) block_max();
+            __syncthreads();
+            if (SORTED) scan_cursors();
+            if (tapmax > 0.0f) bound = ldexpf(cta_max(s_part), -sc);
+            if (SORTED) {
+                __syncthreads();
+                place(key, n);
+                __syncthreads();
+            }
+        } else {
+            for (int i = tid; i < NB * NB; i += kThreadsR) s_blk[i] = 0u;
+            float vmax = 0.0f;
+            for (unsigned i = r0 + tid; i < r1; i += kThreadsR) {
+                const uint4 q = __ldcg(rec + off + i);
+                vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(q.z)), fabsf(__uint_as_float(q.w))));
+            }
+            warp_vmax(vmax);
+            __syncthreads();
+            tapmax = cta_max(s_vmax);
+            if (tapmax > 0.0f) {
+                const int sc = sum_scale(tapmax);
+                const float up = ldexpf(1.0f, sc);
+                for (unsigned i = r0 + tid; i < r1; i += kThreadsR) add_block(__ldcg(rec + off + i), up);
+                __syncthreads();
+                block_max();
+                __syncthreads();
+                bound = ldexpf(cta_max(s_part), -sc);
+            }
         }
         // cell sums stay below 2^30 (+ at most one rounding per term) and
         // every scaled tap below 2^22 (exact rounding with one FMA, below)
@@ -287,67 +403,37 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
         const float scale = ldexpf(1.0f, fexp);
         const float inv = ldexpf(1.0f, -fexp);
 
-        const unsigned n = r1 - r0;
-        const unsigned nst = (n + kStageR - 1) / kStageR;
+        const unsigned nst = one_stage ? 1u : (n + kStageR - 1) / kStageR;
         const unsigned per = nst ? (n + nst - 1) / nst : 0u;
         for (unsigned st = 0; st < nst; st++) {
             const unsigned c0 = r0 + st * per;
             const unsigned cnt = min(per, r1 - c0);
-            __syncthreads();   // the previous stage's streams are done with stage/sidx
-            for (int i = tid; i < NKEY / 2; i += kThreadsR) hist[i] = 0u;
-            unsigned key[RPT];
+            if (!one_stage) {
+                __syncthreads();   // the previous stage's streams are done with stage/sidx
+                if (SORTED)
+                    for (int i = tid; i < NKEY / 2; i += kThreadsR) hist[i] = 0u;
 #pragma unroll
-            for (int t = 0; t < RPT; t++) {
-                const unsigned i = tid + t * kThreadsR;
-                key[t] = 0u;
-                if (i < cnt) {
-                    const uint4 q = __ldcs(rec + off + c0 + i);
-                    stage[i] = q;
-                    key[t] = cell_key<T>(q);
+                for (int t = 0; t < RPT; t++) {
+                    const unsigned i = tid + t * kThreadsR;
+                    key[t] = 0u;
+                    if (i < cnt) {
+                        const uint4 q = __ldcs(rec + off + c0 + i);
+                        stage[i] = q;
+                        if (SORTED) key[t] = cell_key<T>(q);
+                    }
                 }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int t = 0; t < RPT; t++)
-                if (tid + t * kThreadsR < cnt)
-                    atomicAdd(&hist[key[t] >> 1], (key[t] & 1u) ? 0x10000u : 1u);
-            __syncthreads();
-            // exclusive scan of the bucket counts (two 16-bit counts per word,
-            // buckets in key order); a cursor never exceeds cnt < 2^16
-            {
-                unsigned wv[KW];
-                unsigned run = 0u;
-#pragma unroll
-                for (int t = 0; t < KW; t++) {
-                    wv[t] = hist[tid * KW + t];
-                    run += (wv[t] & 0xFFFFu) + (wv[t] >> 16);
-                }
-                unsigned incl = run;
-                for (int d = 1; d < 32; d <<= 1) {
-                    const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-                    if (lane >= d) incl += y;
-                }
-                if (lane == 31) s_wsum[warp] = incl;
                 __syncthreads();
-                unsigned base = incl - run;
-                for (int i = 0; i < warp; i++) base += s_wsum[i];
-#pragma unroll
-                for (int t = 0; t < KW; t++) {
-                    const unsigned lo = wv[t] & 0xFFFFu, hi = wv[t] >> 16;
-                    hist[tid * KW + t] = base | ((base + lo) << 16);
-                    base += lo + hi;
+                if (SORTED) {
+                    count_keys(key, cnt);
+                    __syncthreads();
+                    scan_warps();
+                    __syncthreads();
+                    scan_cursors();
+                    __syncthreads();
+                    place(key, cnt);
+                    __syncthreads();
                 }
             }
-            __syncthreads();
-#pragma unroll
-            for (int t = 0; t < RPT; t++) {
-                const unsigned i = tid + t * kThreadsR;
-                if (i < cnt) {
-                    const unsigned old = atomicAdd(&hist[key[t] >> 1], (key[t] & 1u) ? 0x10000u : 1u);
-                    sidx[(key[t] & 1u) ? (old >> 16) : (old & 0xFFFFu)] = (unsigned short)i;
-                }
-            }
-            __syncthreads();
 
             // the streams
             const unsigned len = (cnt + NS - 1) / NS;
@@ -359,7 +445,7 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
             for (unsigned t = 0; t < len; t++) {
                 const unsigned ri = sbeg + t;
                 const bool valid = lane_on && ri < cnt;
-                const uint4 q = stage[sidx[valid ? ri : 0u]];
+                const uint4 q = stage[SORTED ? sidx[valid ? ri : 0u] : (valid ? ri : 0u)];
                 const int cu = (int)(q.x >> 24) - 64;
                 const int cv = (int)(q.y >> 24) - 64;
                 const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
@@ -661,19 +747,20 @@ template <int T, int K> size_t grid_smem(int prec)
            (size_t)kStageR * sizeof(unsigned short);
 }
 
-template <int T, int K> const void *grid_kernel(int prec)
+template <int T, int K> const void *grid_kernel(int prec, bool tracks)
 {
-    return prec == WSG_FP64 ? (const void *)k_grid_f64<T, K> : (const void *)k_grid_f32c<T, K>;
+    if (prec == WSG_FP64) return (const void *)k_grid_f64<T, K>;
+    return tracks ? (const void *)k_grid_f32c<T, K, false> : (const void *)k_grid_f32c<T, K, true>;
 }
 
 template <int T>
-const void *grid_select(int prec, int half, size_t &smem)
+const void *grid_select(int prec, int half, bool tracks, size_t &smem)
 {
     switch (half) {
 #define WSG_CASE(KK)                           \
     case KK:                                   \
         smem = grid_smem<T, KK>(prec);         \
-        return grid_kernel<T, KK>(prec);
+        return grid_kernel<T, KK>(prec, tracks);
         WSG_CASE(0) WSG_CASE(1) WSG_CASE(2) WSG_CASE(3)
         WSG_CASE(4) WSG_CASE(5) WSG_CASE(6) WSG_CASE(7)
 #undef WSG_CASE
@@ -681,10 +768,10 @@ const void *grid_select(int prec, int half, size_t &smem)
     return nullptr;
 }
 
-const void *grid_pick(int prec, int tile, int half, size_t &smem)
+const void *grid_pick(int prec, int tile, int half, bool tracks, size_t &smem)
 {
-    if (tile == 32) return grid_select<32>(prec, half, smem);
-    if (tile == 64) return grid_select<64>(prec, half, smem);
+    if (tile == 32) return grid_select<32>(prec, half, tracks, smem);
+    if (tile == 64) return grid_select<64>(prec, half, tracks, smem);
     return nullptr;
 }
 
@@ -693,7 +780,7 @@ const void *grid_pick(int prec, int tile, int half, size_t &smem)
 int grid_max_ctas_per_sm(int prec, int tile, int half)
 {
     size_t smem = 0;
-    const void *k = grid_pick(prec, tile, half, smem);
+    const void *k = grid_pick(prec, tile, half, false, smem);
     if (!k) return 0;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
@@ -706,10 +793,11 @@ int grid_max_ctas_per_sm(int prec, int tile, int half)
 }
 
 cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b, const RecBuffers &r,
-                        void *grid, void *partials, int ctas, cudaStream_t s, bool sparse)
+                        void *grid, void *partials, int ctas, cudaStream_t s, bool sparse,
+                        bool tracks)
 {
     size_t smem = 0;
-    const void *k = grid_pick(prec, g.tile, g.half, smem);
+    const void *k = grid_pick(prec, g.tile, g.half, tracks, smem);
     if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

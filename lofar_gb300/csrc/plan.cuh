@@ -84,6 +84,7 @@ struct wsg_plan {
     cudaStream_t stream = nullptr;
     int tile = 64, ctas_grid = 0, ctas_degrid = 0, split = wsg::kDefaultSplit, ctas_user = 0;
     long long rows = 0;   // measurements per dump of the inputs' layout (0 = unknown)
+    bool walked = false;  // the binned records came from the [dump][baseline] walk
     wsg::GeomParams geom{};
 
     wsg::DevBuf grid;                          // resident [jobs*P][Ny][Nx] complex

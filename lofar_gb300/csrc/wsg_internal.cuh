@@ -159,6 +159,10 @@ struct WScreen {
 };
 
 // ---- launchers (bin.cu) ----
+// The single-image binning walks [dump][baseline] tiles (g.rows rows per
+// dump) instead of index order.
+inline bool rows_walk(const GeomParams &g, long long n) { return g.rows > 1 && g.rows < n; }
+
 cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double *vv,
                              const double *ww, long long n, const BinBuffers &b,
                              cudaStream_t s);
@@ -196,9 +200,12 @@ cudaError_t launch_bin_scatter_batch(const GeomParams &g, int prec, const ChanTa
 // sparse: FP32C only; grids the occupied bins alone and leaves the tiles of
 // empty bins unwritten (for the fused imaging path, whose column transforms
 // read occupied tiles only).  Otherwise every tile of the grid is written.
+// tracks: FP32C only; the records were binned by the [dump][baseline] walk
+// (rows_walk), so each bin holds tracks in dump order and the stages are
+// used as stored instead of sorted by cell (the grid is the same).
 cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b,
                         const RecBuffers &r, void *grid, void *partials, int ctas,
-                        cudaStream_t s, bool sparse = false);
+                        cudaStream_t s, bool sparse = false, bool tracks = false);
 int grid_max_ctas_per_sm(int prec, int tile, int half);
 
 // ---- launchers (degrid.cu) ----
