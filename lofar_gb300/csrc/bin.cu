@@ -399,16 +399,36 @@ __device__ __forceinline__ long long rows_m(const RowsWalk &w, unsigned tb, unsi
     return (bl < w.rows && m < w.n) ? m : -1;
 }
 
-// Loads the coordinates of dump t, baseline j of walk tile q (zeros outside
+// Walk tile q = tb * nbb + bb (tb: block of 32 dumps, bb: block of 8
+// baselines).  A CTA's tiles advance by the grid stride, one division ahead
+// of the loop and none in it.
+struct WalkPos {
+    unsigned tb, bb;
+};
+__device__ __forceinline__ WalkPos walk_pos(const RowsWalk &w, unsigned q)
+{
+    const unsigned tb = q / w.nbb;
+    return {tb, q - tb * w.nbb};
+}
+__device__ __forceinline__ void walk_advance(const RowsWalk &w, WalkPos &p, const WalkPos &step)
+{
+    p.tb += step.tb;
+    p.bb += step.bb;
+    if (p.bb >= w.nbb) {
+        p.bb -= w.nbb;
+        p.tb += 1u;
+    }
+}
+
+// Loads the coordinates of dump t, baseline j of walk tile p (zeros outside
 // the measurements); returns the measurement's index, or -1.
-__device__ __forceinline__ long long rows_load3(const RowsWalk &w, long long q, int t, int j,
+__device__ __forceinline__ long long rows_load3(const RowsWalk &w, const WalkPos &p, int t, int j,
                                                const double *__restrict__ uu,
                                                const double *__restrict__ vv,
                                                const double *__restrict__ ww, double &u, double &v,
                                                double &x)
 {
-    const unsigned tb = (unsigned)(q / w.nbb), bb = (unsigned)(q - (long long)tb * w.nbb);
-    const long long m = rows_m(w, tb, bb, t, j);
+    const long long m = rows_m(w, p.tb, p.bb, t, j);
     u = m >= 0 ? __ldcs(uu + m) : 0.0;
     v = m >= 0 ? __ldcs(vv + m) : 0.0;
     x = m >= 0 ? __ldcs(ww + m) : 0.0;
@@ -427,15 +447,18 @@ k_bin_count_rows(GeomParams g, const double *__restrict__ uu, const double *__re
     // the next tile's coordinates are loaded into registers while the
     // current tile is processed
     double pu = 0.0, pv = 0.0, pw = 0.0;
-    if ((long long)blockIdx.x < wk.tiles) rows_load3(wk, blockIdx.x, lt, lj, uu, vv, ww, pu, pv, pw);
+    const WalkPos step = walk_pos(wk, gridDim.x);
+    WalkPos cur = walk_pos(wk, blockIdx.x), nxt = cur;
+    walk_advance(wk, nxt, step);
+    if ((long long)blockIdx.x < wk.tiles) rows_load3(wk, cur, lt, lj, uu, vv, ww, pu, pv, pw);
+    int ndp = 0, ndw = 0;   // this thread's measurements outside the planes / the grid
     for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
-        const unsigned tb = (unsigned)(q / wk.nbb), bb = (unsigned)(q - (long long)tb * wk.nbb);
         su[lt][lj] = pu;
         sv[lt][lj] = pv;
         sw[lt][lj] = pw;
         __syncthreads();
-        if (q + gridDim.x < wk.tiles) rows_load3(wk, q + gridDim.x, lt, lj, uu, vv, ww, pu, pv, pw);
-        const long long m = rows_m(wk, tb, bb, lane, warp);
+        if (q + gridDim.x < wk.tiles) rows_load3(wk, nxt, lt, lj, uu, vv, ww, pu, pv, pw);
+        const long long m = rows_m(wk, cur.tb, cur.bb, lane, warp);
         MGeom o;
         const int st = m >= 0 ? measure_cells<UP2, WP2>(g, su[lane][warp], sv[lane][warp],
                                                          sw[lane][warp], o)
@@ -451,16 +474,19 @@ k_bin_count_rows(GeomParams g, const double *__restrict__ uu, const double *__re
             warp_runs(key[d], lane, lead, cnt, rank);
             if (key[d] != kFull && lane == lead) atomicAdd(&b.sub_prim[key[d]], cnt);
         }
-        int ndp = st == 1, ndw = st == 2;
-        for (int d = 16; d >= 1; d >>= 1) {
-            ndp += __shfl_xor_sync(kFull, ndp, d);
-            ndw += __shfl_xor_sync(kFull, ndw, d);
-        }
-        if (lane == 0) {
-            if (ndp) atomicAdd(&b.ctr->dropped_plane, (unsigned long long)ndp);
-            if (ndw) atomicAdd(&b.ctr->dropped_window, (unsigned long long)ndw);
-        }
+        ndp += st == 1;
+        ndw += st == 2;
         __syncthreads();   // the tile's inputs are read before the next tile's land
+        cur = nxt;
+        walk_advance(wk, nxt, step);
+    }
+    for (int d = 16; d >= 1; d >>= 1) {
+        ndp += __shfl_xor_sync(kFull, ndp, d);
+        ndw += __shfl_xor_sync(kFull, ndw, d);
+    }
+    if (lane == 0) {
+        if (ndp) atomicAdd(&b.ctr->dropped_plane, (unsigned long long)ndp);
+        if (ndw) atomicAdd(&b.ctr->dropped_window, (unsigned long long)ndw);
     }
 }
 
@@ -471,7 +497,7 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
                    const float *__restrict__ vi, const float *__restrict__ wt, RowsWalk wk,
                    long long nf, long long np, BinBuffers b, RecBuffers r)
 {
-    using S = typename std::conditional<PREC == WSG_FP64, double, float>::type;
+    static_assert(PREC == WSG_FP32C, "the walk serves FP32C plans");
     __shared__ double su[32][9], sv[32][9], sw[32][9];
     __shared__ float sr[32][9], si[32][9], st_[32][9];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -482,15 +508,17 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
     // is processed
     double pu = 0.0, pv = 0.0, pw = 0.0;
     float pr = 0.0f, pi = 0.0f, pt = 0.0f;
-    auto load = [&](long long qq) {
-        const long long mm = rows_load3(wk, qq, lt, lj, uu, vv, ww, pu, pv, pw);
+    auto load = [&](const WalkPos &pp) {
+        const long long mm = rows_load3(wk, pp, lt, lj, uu, vv, ww, pu, pv, pw);
         pr = (single && mm >= 0) ? __ldcs(vr + mm) : 0.0f;
         pi = (single && mm >= 0) ? __ldcs(vi + mm) : 0.0f;
         pt = (single && mm >= 0) ? __ldcs(wt + mm) : 0.0f;
     };
-    if ((long long)blockIdx.x < wk.tiles) load(blockIdx.x);
+    const WalkPos step = walk_pos(wk, gridDim.x);
+    WalkPos cur = walk_pos(wk, blockIdx.x), nxt = cur;
+    walk_advance(wk, nxt, step);
+    if ((long long)blockIdx.x < wk.tiles) load(cur);
     for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
-        const unsigned tb = (unsigned)(q / wk.nbb), bb = (unsigned)(q - (long long)tb * wk.nbb);
         su[lt][lj] = pu;
         sv[lt][lj] = pv;
         sw[lt][lj] = pw;
@@ -498,8 +526,8 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
         si[lt][lj] = pi;
         st_[lt][lj] = pt;
         __syncthreads();
-        if (q + gridDim.x < wk.tiles) load(q + gridDim.x);
-        const long long m = rows_m(wk, tb, bb, lane, warp);
+        if (q + gridDim.x < wk.tiles) load(nxt);
+        const long long m = rows_m(wk, cur.tb, cur.bb, lane, warp);
         const double x = su[lane][warp], y = sv[lane][warp], z = sw[lane][warp];
         MGeom o;
         const int st = m >= 0 ? measure_cells<UP2, WP2>(g, x, y, z, o) : 3;
@@ -527,23 +555,18 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
             pos[d] = key[d] != kFull ? base + (lr[d] & 0xFFu) : kFull;
         }
         if (st == 0) {
-            S fu = 0, fv = 0;
             unsigned qu = 0u, qv = 0u;
-            if (PREC == WSG_FP64) {
-                measure<UP2, WP2, S>(g, x, y, z, o, fu, fv);
-            } else {
-                bool ok;
-                coord_cell_q24<UP2>(x, g.ku, g.dx, qu, ok);
-                coord_cell_q24<UP2>(y, g.ku, g.dx, qv, ok);
-            }
-            S re, im;
+            bool ok;
+            coord_cell_q24<UP2>(x, g.ku, g.dx, qu, ok);
+            coord_cell_q24<UP2>(y, g.ku, g.dx, qv, ok);
+            float re, im;
             if (single) {
                 // the fold of w-stacking.cu:98-112 with one entry
                 const float a = sr[lane][warp], w = st_[lane][warp];
-                re = isnan(a) ? (S)0 : (S)(w * a);
-                im = isnan(a) ? (S)0 : (S)(w * si[lane][warp]);
+                re = isnan(a) ? 0.0f : w * a;
+                im = isnan(a) ? 0.0f : w * si[lane][warp];
             } else {
-                fold_value<S>(vr, vi, wt, m, nf, np, re, im);
+                fold_value<float>(vr, vi, wt, m, nf, np, re, im);
             }
 #pragma unroll
             for (int d = 0; d < 4; d++) {
@@ -552,20 +575,16 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
                 const int tu = o.tu0 + (d & 1), tv = o.tv0 + (d >> 1);
                 const int cu = o.gu - (tu << g.tile_shift);
                 const int cv = o.gv - (tv << g.tile_shift);
-                if (PREC == WSG_FP64) {
-                    r.cell[p] = (unsigned)(cu + 32768) | ((unsigned)(cv + 32768) << 16);
-                    reinterpret_cast<double2 *>(r.frac)[p] = make_double2(fu, fv);
-                    reinterpret_cast<double2 *>(r.val)[p] = make_double2(re, im);
-                } else {
-                    r.rec16[p] = make_uint4(((unsigned)(cu + 64) << 24) | qu,
-                                            ((unsigned)(cv + 64) << 24) | qv,
-                                            __float_as_uint((float)re), __float_as_uint((float)im));
-                }
+                r.rec16[p] = make_uint4(((unsigned)(cu + 64) << 24) | qu,
+                                        ((unsigned)(cv + 64) << 24) | qv, __float_as_uint(re),
+                                        __float_as_uint(im));
                 // only the degridder reads idx, and only of primaries
                 if (d == dp) r.idx[p] = (unsigned)m;
             }
         }
         __syncthreads();   // the tile's inputs are read before the next tile's land
+        cur = nxt;
+        walk_advance(wk, nxt, step);
     }
 }
 
@@ -973,18 +992,21 @@ static void scatter_dispatch(const GeomParams &g, const double *uu, const double
                              const float *wt, long long n, long long nf, long long np,
                              const BinBuffers &b, const RecBuffers &r, cudaStream_t s)
 {
-    if (rows_walk(g, n)) {
-        const RowsWalk w = make_rows_walk(n, g.rows);
-        const int blocks = tile_grid(w.tiles);
-        if (g.u_pow2 && g.w_pow2)
-            k_bin_scatter_rows<true, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
-        else if (g.u_pow2)
-            k_bin_scatter_rows<true, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
-        else if (g.w_pow2)
-            k_bin_scatter_rows<false, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
-        else
-            k_bin_scatter_rows<false, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
-        return;
+    // FP32C plans only (the plan keeps g.rows at 0 for FP64)
+    if constexpr (PREC != WSG_FP64) {
+        if (rows_walk(g, n)) {
+            const RowsWalk w = make_rows_walk(n, g.rows);
+            const int blocks = tile_grid(w.tiles);
+            if (g.u_pow2 && g.w_pow2)
+                k_bin_scatter_rows<true, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+            else if (g.u_pow2)
+                k_bin_scatter_rows<true, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+            else if (g.w_pow2)
+                k_bin_scatter_rows<false, true, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+            else
+                k_bin_scatter_rows<false, false, PREC><<<blocks, 256, 0, s>>>(g, uu, vv, ww, vr, vi, wt, w, nf, np, b, r);
+            return;
+        }
     }
     const long long tiles = (n + 256 * kItemsScatter - 1) / (256 * kItemsScatter);
     const int blocks = tile_grid(tiles);
