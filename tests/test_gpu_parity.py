@@ -289,3 +289,48 @@ def test_layout_hint_changes_only_the_walk(medium, precision):
         else:
             assert _nrm_rms(g, medium["grid"]) <= 1e-6, rows
             assert _nrm_max(g, medium["grid"]) <= 1e-5, rows
+
+
+def test_layout_walk_grids_the_same_bits_and_counts():
+    """The [dump][baseline] walk bins the same records as the index-order walk.
+    Without split bins the FP32C grid is then bit-identical (integer tile sums
+    at an order-independent scale), whatever rows count the plan is given: the
+    true one (n not a multiple of it), a wrong one, n - 1 (two dumps, the last
+    of one row) or more than n (index order).  The dropped-measurement counts
+    agree.  The inputs hold measurements outside the planes and outside the
+    grid, and NaN values; the walk's grid matches the oracle."""
+    import torch
+    from lofar_gb300 import Plan, synth
+    o = synth.observe(n_stations=20, diameter_m=3000.0, hours=3.0, n_vis=190_001)
+    uu, vv, ww = o.uu.copy(), o.vv.copy(), o.ww.copy()
+    vr, vi, wt = o.vis_real.copy(), o.vis_img.copy(), o.weight.copy()
+    n, nb = uu.shape[0], o.meta["n_baselines"]
+    assert n % nb != 0
+    ww[::997] = 1.5          # past the last plane
+    uu[5::1009] = 3.0        # window entirely outside the grid
+    vr[7::1013] = np.nan     # contributes zero (w-stacking.cu:98-112)
+    nx, planes = 256, 8
+    first = None
+    for rows in (nb, 0, 3, n - 1, n + 5):
+        p = Plan(nx, nx, planes, 7, precision="fp32c")
+        p.set_tuning(chunk=1 << 22)   # no bin is split
+        p.set_layout(rows)
+        p.bin(uu, vv, ww, vr, vi, wt)
+        g = torch.view_as_real(p.grid()).cpu()
+        st = p.stats()
+        p.close()
+        assert st["max_bin_records"] < (1 << 22)
+        if first is None:
+            first = (g, st)
+            keep = ww < 1.0   # the oracle, like the reference, takes in-range planes only
+            ref = O.wstack(uu[keep], vv[keep], ww[keep], vr[keep], vi[keep], wt[keep],
+                           num_w_planes=planes, dx=1 / nx, dw=1 / planes, w_support=7, nx=nx,
+                           ny=nx)
+            assert _nrm_rms(g.double().numpy(), ref) <= 1e-6
+            assert _nrm_max(g.double().numpy(), ref) <= 1e-5
+            assert st["dropped_plane"] == len(range(0, n, 997))
+            assert st["dropped_window"] > 0
+            continue
+        assert torch.equal(g, first[0]), rows
+        for k in ("points_in", "records", "dropped_plane", "dropped_window"):
+            assert st[k] == first[1][k], (rows, k)
