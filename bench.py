@@ -159,8 +159,9 @@ def algorithmic_bytes(n, nx, ny, planes, sc):
 
 
 PROFILE_MD = os.path.join(ROOT, "profiles", "launches_fwd_adj_4096x32_50M.md")
-GRIDDING_KERNELS = ("k_bin_count", "k_bin_scan_a", "k_bin_scan_b", "k_bin_scan_c",
-                    "k_bin_scatter", "k_fft_masks", "k_grid_f32c")
+GRIDDING_KERNELS = ("k_bin_count", "k_bin_count_rows", "k_bin_scan_a", "k_bin_scan_b",
+                    "k_bin_scan_c", "k_bin_scatter", "k_bin_scatter_rows", "k_fft_masks",
+                    "k_grid_f32c")
 PROFILE_RECORDS = 59_834_420   # records binned in the profiled run (4096^2 x 32, 50M)
 
 
@@ -181,7 +182,7 @@ def profiled_traffic(records):
                 seen.add(name)
             except ValueError:
                 pass
-    if "k_grid_f32c" not in seen or "k_bin_scatter" not in seen:
+    if "k_grid_f32c" not in seen or not seen & {"k_bin_scatter", "k_bin_scatter_rows"}:
         return None
     return tot * records / PROFILE_RECORDS
 
