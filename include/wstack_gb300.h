@@ -154,9 +154,12 @@ WSG_API int wsg_plan_set_tuning(wsg_plan *plan, int tile, int ctas, int chunk);
  * per dump, as the reference's measurement sets are written (meta.txt's
  * `baselines`, init.c:293).  An FP32C plan's binning then walks each
  * baseline's consecutive dumps together, so records that share a bin merge
- * their cursor atomics and are written contiguously.  A speed hint only: the
- * grid does not depend on it (a wrong count only changes the speed); FP64
- * plans keep the index-order walk; 0 (the default) walks in index order. */
+ * their cursor atomics and are written contiguously, and the gridder sums
+ * the records of each track as stored instead of sorting them by cell.  A
+ * speed hint: the grid is bit-identical when no bin is split into chunks and
+ * otherwise differs only by the FP32C rounding of the chunks' partial tiles;
+ * a wrong count only changes the speed.  FP64 plans keep the index-order
+ * walk; 0 (the default) walks in index order. */
 WSG_API int wsg_plan_set_layout(wsg_plan *plan, long rows_per_dump);
 /* Reserves device memory for up to max_points measurements so that later
  * calls allocate nothing (required before CUDA-graph capture). */
