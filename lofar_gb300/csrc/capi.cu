@@ -105,13 +105,11 @@ int wsg::num_sms()
 WScreen wsg::plan_wscreen(const wsg_plan *p)
 {
     WScreen ws;
-    float *base = p->wscreen.as<float>();
+    unsigned *base = p->wscreen.as<unsigned>();
     const long long n = p->npix();
-    ws.ah = base;
-    ws.al = base ? base + n : nullptr;
-    ws.bh = base ? base + 2 * n : nullptr;
-    ws.bl = base ? base + 3 * n : nullptr;
-    ws.amp = base ? base + 4 * n : nullptr;
+    ws.aq = base;
+    ws.bq = base ? base + n : nullptr;
+    ws.amp = base ? reinterpret_cast<float *>(base + 2 * n) : nullptr;
     ws.sinx = p->sinx.as<double>();
     ws.siny = p->siny.as<double>();
     return ws;
@@ -255,7 +253,7 @@ int wsg::ensure_wscreen(wsg_plan *p)
     WSG_CUDA(p->siny.ensure(sizeof(double) * p->ny));
     WSG_CUDA(launch_wscreen_tables(p->wc, p->sinx.as<double>(), p->siny.as<double>(), p->stream));
     if (p->prec == WSG_FP32C && p->wc.phase_on && p->planes > 1) {
-        WSG_CUDA(p->wscreen.ensure(sizeof(float) * 5 * (size_t)p->npix()));
+        WSG_CUDA(p->wscreen.ensure(sizeof(unsigned) * 3 * (size_t)p->npix()));
         WSG_CUDA(launch_wscreen_build(p->wc, plan_wscreen(p), p->stream));
     }
     p->ws_ready = true;

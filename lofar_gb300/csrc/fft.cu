@@ -630,19 +630,6 @@ struct RowArgs {
     FftMasks m;
 };
 
-__device__ __forceinline__ float cycle_frac_f(float ah, float al, float bh, float bl, float wf)
-{
-    const float p = wf * bh;
-    const float pe = fmaf(wf, bh, -p);
-    const float s = ah + p;
-    const float z = s - ah;
-    const float se = (ah - (s - z)) + (p - z);
-    const float lo = fmaf(wf, bl, al) + (pe + se);
-    return (s - rintf(s)) + lo;
-}
-
-constexpr float kTwoPi = 6.28318530717958647692f;
-
 // Forward: one image row.  For every plane: row FFT (exponent +i), w-term
 // phase, plane sum.  Grid: y = image row.
 template <int N>
@@ -652,8 +639,8 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
     constexpr int Q = N / T;   // pixels per thread
     extern __shared__ __align__(16) unsigned char rsm[];
     float2 *buf = reinterpret_cast<float2 *>(rsm);
-    float *wah = reinterpret_cast<float *>(rsm + ((FftPlan<N>::PAD * 8 + 15) / 16) * 16);
-    float *wal = wah + N, *wbh = wal + N, *wbl = wbh + N;
+    // the row's w-screen: Q32 cycle fractions (aq, bq) per pixel
+    uint2 *wq = reinterpret_cast<uint2 *>(rsm + ((FftPlan<N>::PAD * 8 + 15) / 16) * 16);
     const int y = blockIdx.x, t = threadIdx.x;
     const size_t prow = (size_t)y * N;
     // job blockIdx.y: its planes, masks and image
@@ -661,15 +648,9 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
     const float2 *gridj = a.grid + jp * a.ny * N;
     const unsigned char *plane_occ = a.m.plane_occ + jp;
     float2 *image = a.image + (size_t)blockIdx.y * a.ny * N;
-    if (a.phase) {
-        for (int x = t; x < N; x += T) {
-            wah[x] = a.ws.ah[prow + x];
-            wal[x] = a.ws.al[prow + x];
-            wbh[x] = a.ws.bh[prow + x];
-            wbl[x] = a.ws.bl[prow + x];
-        }
-    }
-    unsigned char *smask = reinterpret_cast<unsigned char *>(wbl + N);   // [planes][ntu]
+    if (a.phase)
+        for (int x = t; x < N; x += T) wq[x] = make_uint2(a.ws.aq[prow + x], a.ws.bq[prow + x]);
+    unsigned char *smask = reinterpret_cast<unsigned char *>(wq + N);   // [planes][ntu]
     for (int i = t; i < a.planes * a.ntu; i += T) smask[i] = a.m.occ_col[jp * a.ntu + i];
     __syncthreads();
     float sr[Q], si[Q];
@@ -698,15 +679,14 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc(RowArgs a)
         if (wn < a.planes) fetch(wn);
         __syncthreads();   // the previous plane's last pass has read buf
         fft_row<N, +1, T, true, true>(fv, buf, t, a.tw);   // the row in and out of registers
-        const float wf = (float)w;
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const int x = t + q * T;
             const float2 v = fv[q];
             if (a.phase) {
-                const float c = cycle_frac_f(wah[x], wal[x], wbh[x], wbl[x], wf);
+                const uint2 c = wq[x];
                 float sn, cs;
-                __sincosf(kTwoPi * c, &sn, &cs);
+                __sincosf(wscreen_angle(c.x, c.y, (unsigned)w), &sn, &cs);
                 sr[q] += v.x * cs - v.y * sn;
                 si[q] += v.x * sn + v.y * cs;
             } else {
@@ -733,23 +713,17 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
     constexpr int Q = N / T;
     extern __shared__ __align__(16) unsigned char rsm[];
     float2 *buf = reinterpret_cast<float2 *>(rsm);
-    float *wah = reinterpret_cast<float *>(rsm + ((FftPlan<N>::PAD * 8 + 15) / 16) * 16);
-    float *wal = wah + N, *wbh = wal + N, *wbl = wbh + N;
+    // the row's w-screen: Q32 cycle fractions (aq, bq) per pixel
+    uint2 *wq = reinterpret_cast<uint2 *>(rsm + ((FftPlan<N>::PAD * 8 + 15) / 16) * 16);
     const int y = blockIdx.x, t = threadIdx.x;
     const size_t prow = (size_t)y * N;
     const size_t jp = (size_t)blockIdx.y * a.planes;
     float2 *gridj = a.grid + jp * a.ny * N;
     const unsigned char *plane_need = a.m.plane_need + jp;
     const float2 *image = a.image + (size_t)blockIdx.y * a.ny * N;
-    if (a.phase) {
-        for (int x = t; x < N; x += T) {
-            wah[x] = a.ws.ah[prow + x];
-            wal[x] = a.ws.al[prow + x];
-            wbh[x] = a.ws.bh[prow + x];
-            wbl[x] = a.ws.bl[prow + x];
-        }
-    }
-    unsigned char *smask = reinterpret_cast<unsigned char *>(wbl + N);   // [planes][ntu]
+    if (a.phase)
+        for (int x = t; x < N; x += T) wq[x] = make_uint2(a.ws.aq[prow + x], a.ws.bq[prow + x]);
+    unsigned char *smask = reinterpret_cast<unsigned char *>(wq + N);   // [planes][ntu]
     for (int i = t; i < a.planes * a.ntu; i += T) smask[i] = a.m.need_col[jp * a.ntu + i];
     float2 im[Q];
 #pragma unroll
@@ -762,7 +736,7 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
             // image may hold NaN there) and a zero phase (their w-screen
             // entries are NaN too)
             im[q] = make_float2(0.f, 0.f);
-            if (a.phase) wah[x] = wal[x] = wbh[x] = wbl[x] = 0.f;
+            if (a.phase) wq[x] = make_uint2(0u, 0u);
         } else {
             im[q] = make_float2(v.x * amp, v.y * amp);
         }
@@ -770,16 +744,15 @@ __global__ void __launch_bounds__(fft_threads<N>()) k_rows_wc_adj(RowArgs a)
     __syncthreads();   // shared w-screen and masks loaded
     for (int w = 0; w < a.planes; w++) {
         if (!plane_need[w]) continue;
-        const float wf = (float)w;
         float2 fv[Q];   // the phased row, then (in place) its transform
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const int x = t + q * T;
             float2 v = im[q];
             if (a.phase) {
-                const float c = cycle_frac_f(wah[x], wal[x], wbh[x], wbl[x], wf);
+                const uint2 c = wq[x];
                 float sn, cs;
-                __sincosf(kTwoPi * c, &sn, &cs);
+                __sincosf(wscreen_angle(c.x, c.y, (unsigned)w), &sn, &cs);
                 v = make_float2(cs * im[q].x + sn * im[q].y, cs * im[q].y - sn * im[q].x);
             }
             fv[q] = v;
@@ -866,7 +839,7 @@ __global__ void k_twiddles(float2 *tw, int n)
 template <int N> size_t col_smem() { return (size_t)kColsPerCta * col_stride<N>() * sizeof(float2); }
 template <int N> size_t row_smem(int planes, int ntu)
 {
-    return ((FftPlan<N>::PAD * 8 + 15) / 16) * 16 + (size_t)4 * N * sizeof(float) +
+    return ((FftPlan<N>::PAD * 8 + 15) / 16) * 16 + (size_t)N * sizeof(uint2) +
            (size_t)planes * ntu;
 }
 

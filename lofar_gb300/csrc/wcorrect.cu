@@ -20,9 +20,9 @@
 // restricted to its finite pixels.
 //
 // FP32C form: per pixel, the phase in cycles a + w*b (mod 1) is tabulated once
-// per plan as reduced float-float pairs (computed in FP64); per plane the
-// fractional cycle is recovered exactly in FP32 with an error-free product
-// and TwoSum, then one hardware sincos of an argument in [-pi, pi].
+// per plan (computed in FP64) as Q32 fractions of a cycle; per plane the cycle
+// fraction is one integer multiply-add, reduced modulo 1 by the 32-bit
+// wrap-around, then one hardware sincos of an argument in [-pi, pi).
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -71,25 +71,11 @@ __global__ void k_wscreen_build(WcParams p, WScreen ws)
         double b = (dw * t) * kappa;
         a -= rint(a);
         b -= rint(b);
-        const float ah = (float)a, bh = (float)b;
-        ws.ah[pix] = ah;
-        ws.al[pix] = (float)(a - (double)ah);
-        ws.bh[pix] = bh;
-        ws.bl[pix] = (float)(b - (double)bh);
+        // |a|, |b| <= 1/2: a * 2^32 rounded to an integer, taken modulo 2^32
+        ws.aq[pix] = (unsigned)llrint(a * 4294967296.0);
+        ws.bq[pix] = (unsigned)llrint(b * 4294967296.0);
         ws.amp[pix] = (float)(dwnorm * s);
     }
-}
-
-// Fractional cycle of a + w*b, |a|,|b| <= 1/2 given as float-float pairs.
-__device__ __forceinline__ float cycle_frac(float ah, float al, float bh, float bl, float wf)
-{
-    const float p = wf * bh;
-    const float pe = fmaf(wf, bh, -p);          // exact product error
-    const float s = ah + p;
-    const float z = s - ah;
-    const float se = (ah - (s - z)) + (p - z);  // TwoSum error
-    const float lo = fmaf(wf, bl, al) + (pe + se);
-    return (s - rintf(s)) + lo;                 // s - rint(s) is exact
 }
 
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x)
@@ -209,8 +195,6 @@ __device__ __forceinline__ double fixed_to_f64(long long v, int k)
     return __longlong_as_double(from_fixed(v, k));
 }
 
-constexpr float kTwoPiF = 6.28318530717958647692f;
-
 __global__ void __launch_bounds__(256)
 k_wcorrect_f32c(WcParams p, WScreen ws, const float2 *__restrict__ planes,
                 float2 *__restrict__ image, float scale)
@@ -221,13 +205,12 @@ k_wcorrect_f32c(WcParams p, WScreen ws, const float2 *__restrict__ planes,
          pix += (long long)gridDim.x * blockDim.x) {
         float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
         if (phase) {
-            const float ah = ws.ah[pix], al = ws.al[pix], bh = ws.bh[pix], bl = ws.bl[pix];
+            const unsigned aq = ws.aq[pix], bq = ws.bq[pix];
 #pragma unroll 8
             for (int w = 0; w < p.planes; w++) {
                 const float2 g = __ldcs(planes + (size_t)w * npix + pix);
-                const float c = cycle_frac(ah, al, bh, bl, (float)w);
                 float sn, cs;
-                __sincosf(kTwoPiF * c, &sn, &cs);
+                __sincosf(wscreen_angle(aq, bq, (unsigned)w), &sn, &cs);
                 two_sum_acc(hr, lr, g.x * cs - g.y * sn);
                 two_sum_acc(hi, li, g.x * sn + g.y * cs);
             }
@@ -255,7 +238,7 @@ k_wcorrect_adj_f32c(WcParams p, WScreen ws, const float2 *__restrict__ image,
          pix += (long long)gridDim.x * blockDim.x) {
         const float2 im = image[pix];
         if (phase) {
-            const float ah = ws.ah[pix], al = ws.al[pix], bh = ws.bh[pix], bl = ws.bl[pix];
+            const unsigned aq = ws.aq[pix], bq = ws.bq[pix];
             const float amp = ws.amp[pix] * scale;
             if (!(amp == amp)) {  // pixel where the forward is NaN: excluded
                 for (int w = 0; w < p.planes; w++)
@@ -265,9 +248,8 @@ k_wcorrect_adj_f32c(WcParams p, WScreen ws, const float2 *__restrict__ image,
             const float xr = im.x * amp, xi = im.y * amp;
 #pragma unroll 8
             for (int w = 0; w < p.planes; w++) {
-                const float c = cycle_frac(ah, al, bh, bl, (float)w);
                 float sn, cs;
-                __sincosf(kTwoPiF * c, &sn, &cs);
+                __sincosf(wscreen_angle(aq, bq, (unsigned)w), &sn, &cs);
                 __stcs(planes + (size_t)w * npix + pix,
                        make_float2(cs * xr + sn * xi, cs * xi - sn * xr));
             }

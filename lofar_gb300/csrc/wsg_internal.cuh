@@ -153,10 +153,23 @@ inline unsigned long long max_slots(unsigned long long records, unsigned split)
 // Pixel-geometry table of the FP32C w-correction (per pixel, planar):
 // the phase in cycles for plane w is a + w*b (mod 1), a and b as
 // float-float pairs reduced to [-0.5, 0.5]; amp = dwnorm*sqrt(1-r^2).
+// FP32C w-screen, per pixel: the phase of plane w in cycles, a + w*b, with a
+// and b reduced modulo 1 and stored as Q32 fractions of a cycle (aq, bq), so
+// that (aq + w*bq) mod 2^32 is the plane's cycle fraction exactly, by integer
+// wrap-around; amp = dwnorm * sqrt(1 - r2) (NaN outside the unit circle).
 struct WScreen {
-    float *ah, *al, *bh, *bl, *amp;
+    unsigned *aq, *bq;
+    float *amp;
     double *sinx, *siny;
 };
+
+// Phase angle of plane w in radians, in [-pi, pi): the Q32 cycle fraction
+// (aq + w*bq) mod 2^32 read as a signed fraction of a cycle.
+__device__ __forceinline__ float wscreen_angle(unsigned aq, unsigned bq, unsigned w)
+{
+    const int c = (int)(aq + w * bq);
+    return (float)c * 1.46291807926715968e-9f;   // 2 pi / 2^32
+}
 
 // ---- launchers (bin.cu) ----
 // The single-image binning walks [dump][baseline] tiles (g.rows rows per
