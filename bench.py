@@ -810,6 +810,7 @@ def bench_large(args, rank, world, peak, peak_kind):
     n, nx, P, S = d["n"], args.nx, args.planes, args.support
     plan = Plan(nx, nx, P, S, precision="fp32c")
     plan.set_wcorrection(d["resolution"], d["wmin"], d["wmax"])
+    plan.set_layout(d["n_baselines"])   # the generator writes [dump][baseline]
     plan.reserve(n)
     image = torch.empty((nx, nx), dtype=torch.complex64, device="cuda")
     out = torch.empty(n, dtype=torch.complex64, device="cuda")
@@ -974,7 +975,8 @@ def bench_driver(args, rank, world, peak, peak_kind):
         binms.write_dataset(ds, uu=host["uu"], vv=host["vv"], ww=host["ww"],
                             weights=host["weight"], vis_real=host["vis_real"],
                             vis_img=host["vis_img"], freq_per_chan=1, polarisations=1,
-                            uvmin=d["uvmin"], uvmax=d["uvmax"], wmin=d["wmin"], wmax=d["wmax"])
+                            baselines=d["n_baselines"], uvmin=d["uvmin"], uvmax=d["uvmax"],
+                            wmin=d["wmin"], wmax=d["wmax"])
         bytes_in = sum(os.path.getsize(os.path.join(ds, f)) for f in os.listdir(ds))
         del host
         sectoring = bench_sectoring(d["vv"], args.nx, S)
