@@ -440,6 +440,29 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
+// Shared-memory writes of the generic proxy made visible to the tensor memory
+// accelerator (each writing thread, before the barrier that precedes a store).
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// box {2 complex, rows, 1 plane} from shared memory to (x, y, z)
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int x, int y,
+                                             int z)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+            reinterpret_cast<unsigned long long>(map)),
+        "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+// Commits this thread's bulk stores and waits until they have read shared memory.
+__device__ __forceinline__ void tma_store_commit_and_wait_read()
+{
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
 // Threads of a column-strip CTA: one per radix-16 butterfly of a column.
 template <int N> __host__ __device__ constexpr int col_threads() { return N / 16 < 512 ? N / 16 : 512; }
 
@@ -452,6 +475,17 @@ __device__ __forceinline__ void st_row2(float2 *p, float2 a, float2 b)
 
 // Columns per column-FFT CTA (1 or 2).
 constexpr int kColsPerCta = 2;
+
+// The transformed strip goes back through shared memory with
+// tensor-memory-accelerator stores (one box per tile row written; the adjoint
+// writes the tiles the degridder reads) instead of 16-byte stores from every
+// thread.
+constexpr bool kTmaStoreFwd = true;
+constexpr bool kTmaStoreAdj = true;
+template <int MODE> __host__ __device__ constexpr bool tma_store_cols()
+{
+    return MODE == kColsFwd ? kTmaStoreFwd : kTmaStoreAdj;
+}
 
 // Column FFTs of a strip of kColsPerCta adjacent columns of one plane (grid: x =
 // strip, y = plane).  Thread t owns butterfly t of every radix-16 pass of both
@@ -565,12 +599,28 @@ __global__ void __launch_bounds__(col_threads<N>(), col_threads<N>() <= 256 ? (M
         if (NC == 2) dft16<S>(xb);
         if (last) {
             // t / ns == 0: outputs go to rows t + r*ns = t + r*NB
+            if constexpr (tma_store_cols<MODE>() && NC == 2) {
+                __syncthreads();   // every thread has read ca/cb, which the strip overwrites
 #pragma unroll
-            for (int r = 0; r < 16; r++) {
-                const int row = t + r * NB;
-                if (MODE != kColsAdj || s_rows[row >> a.tsh]) {
-                    if (NC == 2) st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
-                    else __stcg(col + (size_t)row * pitch, xa[r]);
+                for (int r = 0; r < 16; r++)
+                    stage[t + r * NB] = make_float4(xa[r].x, xa[r].y, xb[r].x, xb[r].y);
+                fence_proxy_async_smem();
+                __syncthreads();
+                if (t == 0) {
+                    const int nbox = N >> a.tsh;
+                    for (int b = 0; b < nbox; b++)
+                        if (MODE != kColsAdj || s_rows[b])
+                            tma_store_3d(&tmap, stage + b * a.tile, x0, b * a.tile, w);
+                    tma_store_commit_and_wait_read();
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < 16; r++) {
+                    const int row = t + r * NB;
+                    if (MODE != kColsAdj || s_rows[row >> a.tsh]) {
+                        if (NC == 2) st_row2(col + (size_t)row * pitch, xa[r], xb[r]);
+                        else __stcg(col + (size_t)row * pitch, xa[r]);
+                    }
                 }
             }
         } else {
@@ -883,8 +933,8 @@ cudaError_t run_cols(const ColArgs &a, int planes, cudaStream_t s)
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     CUtensorMap m;
-    memset(&m, 0, sizeof(m));   // unused by the forward
-    if (MODE != kColsFwd) {
+    memset(&m, 0, sizeof(m));   // unused by a forward without tensor stores
+    if (MODE != kColsFwd || kTmaStoreFwd) {
         e = cols_tensor_map(a, planes, &m);
         if (e != cudaSuccess) return e;
     }
