@@ -254,20 +254,38 @@ OUR_KERNELS_PER_STEP = {"bin": 6, "grid": 1, "fft_wcorrect": 2, "wcorrect_adj_ff
                         "degrid": 1}
 
 
-def run_plan_steps(plan, ins, image, out, steps, record_stages, reduce=None):
+L2_BYTES = 129 * 1000 * 1000   # GB300 L2
+
+
+def l2_flush_bytes(working_set):
+    """Bytes to write between timed steps so that no step starts with the
+    previous step's data in L2: 0 when the step's working set (inputs, grid)
+    is over twice the L2, else 256 MB."""
+    return 0 if working_set > 2 * L2_BYTES else 256 << 20
+
+
+def l2_note(flush):
+    return ("L2 flushed before every step (256 MB written outside the timed region)" if flush
+            else "inputs larger than L2 (no flush)")
+
+
+def run_plan_steps(plan, ins, image, out, steps, record_stages, reduce=None, flush=0):
     """`steps` forward+adjoint passes; returns (total_ms, {stage: [ms per step]}).
     reduce: applied to the forward image before the adjoint (the plane-sharded
-    form's sum over ranks)."""
+    form's sum over ranks).  flush: bytes written before every step, outside
+    the timed region (the total is then the sum of the steps' own times)."""
     import torch
     stream = torch.cuda.current_stream()
     per = {s: [] for s in STAGES}
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(STAGES) + 1)] if record_stages else None
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    npix = plan.nx * plan.ny
+    scratch = torch.empty(flush, dtype=torch.uint8, device="cuda") if flush else None
     pending = []
     start.record(stream)
     for _ in range(steps):
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(STAGES) + 1)] if record_stages else None
+        if scratch is not None:
+            scratch.zero_()
+        evs = ([torch.cuda.Event(enable_timing=True) for _ in range(len(STAGES) + 1)]
+               if record_stages or flush else None)
         if evs:
             evs[0].record(stream)
         plan.bin(*ins)
@@ -293,6 +311,8 @@ def run_plan_steps(plan, ins, image, out, steps, record_stages, reduce=None):
     for evs in pending:
         for i, s in enumerate(STAGES):
             per[s].append(evs[i].elapsed_time(evs[i + 1]))
+    if flush:
+        return sum(evs[0].elapsed_time(evs[-1]) for evs in pending), per
     return start.elapsed_time(stop), per
 
 
@@ -346,13 +366,14 @@ def bench_ours(args, rank, world):
     # warm-up (also builds the w-screen table and the cuFFT plan)
     run_plan_steps(plan, ins, image, out, args.warmup, False, reduce)
     stats = plan.stats()
+    flush = l2_flush_bytes(n_local * 36 + P * nx * ny * 8)
 
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(dev)
     clocks.start()
-    total_ms, per = run_plan_steps(plan, ins, image, out, args.steps, True, reduce)
+    total_ms, per = run_plan_steps(plan, ins, image, out, args.steps, True, reduce, flush)
     clk = clocks.stop()
     total_ms = max_over_ranks(total_ms, world)
     ms_per_step = total_ms / args.steps
@@ -369,7 +390,7 @@ def bench_ours(args, rank, world):
 
     result = dict(rank=rank, n=n, res=res, wmin=obs.wmin, wmax=obs.wmax, gen_s=gen_s,
                   ms_per_step=ms_per_step, value=value, per=per, stats=stats, clocks=clk,
-                  plan_bytes=plan.device_bytes())
+                  plan_bytes=plan.device_bytes(), l2=l2_note(flush))
 
     # -- plain FP64 form, same inputs --------------------------------------
     if not args.no_fp64 and rank == 0:
@@ -382,7 +403,8 @@ def bench_ours(args, rank, world):
         image64 = torch.empty((ny, nx), dtype=torch.complex128, device="cuda")
         out64 = torch.empty(n, dtype=torch.complex128, device="cuda")
         run_plan_steps(p64, ins, image64, out64, 1, False)
-        ms64, per64 = run_plan_steps(p64, ins, image64, out64, args.fp64_steps, True)
+        ms64, per64 = run_plan_steps(p64, ins, image64, out64, args.fp64_steps, True,
+                                     flush=l2_flush_bytes(n * 36 + P * nx * ny * 16))
         img64 = p64.image_forward(*ins)
         torch.cuda.synchronize()
         a = torch.view_as_real(img32).double()
@@ -1126,7 +1148,7 @@ def main():
                    "precision": "FP32 complex grid, int32 fixed-point tile sums, FP64-exact "
                                 "coordinates and phase argument",
                    "parallelism": (f"planes{world}" if "planes" in res else f"replicas{world}"),
-                   "l2": "inputs larger than L2 (no flush)"},
+                   "l2": res.get("l2", "inputs larger than L2 (no flush)")},
         "roofline": {"bound": "hbm", "kernel": "gridding stage (bin_count+bin_scan+bin_scatter+grid)",
                      "achieved": g["gbs"], "peak": peak, "unit": "GB/s", "frac": g["frac"],
                      "peak_source": f"{peak_kind} hbm copy bandwidth",
