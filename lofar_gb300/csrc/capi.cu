@@ -239,6 +239,11 @@ int wsg::ensure_fused(wsg_plan *p)
         WSG_CUDA(launch_twiddles(p->twy.as<float2>(), p->ny, p->stream));
         p->tw_ready = true;
     }
+    return ensure_masks(p);
+}
+
+int wsg::ensure_masks(wsg_plan *p)
+{
     const size_t nt = (size_t)p->cube_planes() * p->geom.ntv * p->geom.ntu;
     const size_t nc = (size_t)p->cube_planes() * p->geom.ntu;
     WSG_CUDA(p->masks.ensure(2 * nt + 2 * nc + 2 * (size_t)p->cube_planes()));
@@ -263,8 +268,10 @@ int wsg::ensure_wscreen(wsg_plan *p)
 int wsg::finish_binning(wsg_plan *p)
 {
     p->masks_valid = false;
-    if (p->fused) {
-        WSG_TRY(ensure_fused(p));
+    if (p->fused || p->fft64) {
+        // the transforms of the imaging calls read (FP32C forward) and write
+        // (adjoint) only the tiles these masks mark
+        WSG_TRY(p->fused ? ensure_fused(p) : ensure_masks(p));
         WSG_CUDA(launch_fft_masks(p->geom, p->binbufs(), mask_view(p), p->stream));
         p->masks_valid = true;
     }
@@ -501,6 +508,33 @@ int wsg_grid_occupied(wsg_plan *p, void *grid)
     return WSG_OK;
 }
 
+// Tile masks serve the FP64 column pass when a CTA's columns (at most 16)
+// share one tile column, and the column's tile mask fits its shared copy.
+static bool fft64_masks_ok(const wsg_plan *p)
+{
+    return p->geom.tile >= 16 && p->ny / p->geom.tile <= p->ny / 16 && p->nx % p->geom.tile == 0 &&
+           p->ny % p->geom.tile == 0;
+}
+
+// The FP64 plan's integer-pipe transform of its cube; `pruned` (adjoint):
+// with the tile masks of the last binning, only the tiles the degridder reads
+// are written.
+static int fft64_planes(wsg_plan *p, void *grid, int sign, bool pruned)
+{
+    if (!p->tw64_ready) {
+        WSG_CUDA(p->tw64x.ensure((size_t)2 * p->nx * sizeof(int4)));
+        WSG_CUDA(p->tw64y.ensure((size_t)2 * p->ny * sizeof(int4)));
+        WSG_CUDA(build_twiddles64(p->tw64x.as<int4>(), p->nx, p->stream));
+        WSG_CUDA(build_twiddles64(p->tw64y.as<int4>(), p->ny, p->stream));
+        p->tw64_ready = true;
+    }
+    const FftMasks m = mask_view(p);
+    WSG_CUDA(launch_fft64(reinterpret_cast<double2 *>(grid), p->nx, p->ny, (int)p->cube_planes(),
+                          sign, p->tw64x.as<int4>(), p->tw64y.as<int4>(), 0, p->stream,
+                          pruned ? &m : nullptr, p->geom.tile_shift));
+    return WSG_OK;
+}
+
 int wsg_fft(wsg_plan *p, void *grid, int sign)
 {
     clear_error();
@@ -512,19 +546,7 @@ int wsg_fft(wsg_plan *p, void *grid, int sign)
                                     p->twy.as<float2>(), sign, p->stream));
         return WSG_OK;
     }
-    if (p->fft64) {
-        if (!p->tw64_ready) {
-            WSG_CUDA(p->tw64x.ensure((size_t)2 * p->nx * sizeof(int4)));
-            WSG_CUDA(p->tw64y.ensure((size_t)2 * p->ny * sizeof(int4)));
-            WSG_CUDA(build_twiddles64(p->tw64x.as<int4>(), p->nx, p->stream));
-            WSG_CUDA(build_twiddles64(p->tw64y.as<int4>(), p->ny, p->stream));
-            p->tw64_ready = true;
-        }
-        WSG_CUDA(launch_fft64(reinterpret_cast<double2 *>(grid), p->nx, p->ny,
-                              (int)p->cube_planes(), sign, p->tw64x.as<int4>(),
-                              p->tw64y.as<int4>(), 0, p->stream));
-        return WSG_OK;
-    }
+    if (p->fft64) return fft64_planes(p, grid, sign, false);
     WSG_TRY(ensure_fft(p));
     WSG_CUFFT(cufftSetStream(p->fft, p->stream));
     const int dir = sign > 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
@@ -624,7 +646,10 @@ int wsg_wcorrect_adjoint_fft(wsg_plan *p, const void *image, void *grid, int pru
     const double scale = 1.0 / (double)p->npix();
     if (!p->fused || !prune) {
         WSG_TRY(wsg_wcorrect_adjoint(p, image, grid, scale));
-        WSG_TRY(wsg_fft(p, grid, -1));
+        if (prune && p->fft64 && p->masks_valid && fft64_masks_ok(p))
+            WSG_TRY(fft64_planes(p, grid, -1, true));
+        else
+            WSG_TRY(wsg_fft(p, grid, -1));
         return WSG_OK;
     }
     WSG_TRY(ensure_fused(p));

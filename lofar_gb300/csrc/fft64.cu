@@ -187,18 +187,37 @@ __device__ __forceinline__ int fft64_shift(unsigned hi)
 // One CTA: NTR transforms of length N of plane blockIdx.y.  COLS: columns
 // blockIdx.x * NTR + t (element stride nx); else rows (contiguous).  The
 // output is scaled by the exact power of two 2^post.
+// Tile masks of the adjoint's column pass (the last): only the tiles with
+// tile[] set are written, and a tile column with col[] clear is skipped.
+struct ColMasks64 {
+    const unsigned char *tile;   // [planes][ntv][ntu]
+    const unsigned char *col;    // [planes][ntu]
+    int ntu, ntv, tsh;
+    bool on;
+};
+
 template <int N, int SIGN, bool COLS>
 __global__ void __launch_bounds__(Fft64Shape<N>::THREADS, Fft64Shape<N>::MINB)
-    k_fft64(double2 *__restrict__ data, int nx, int ny, const int4 *__restrict__ tw, int post)
+    k_fft64(double2 *__restrict__ data, int nx, int ny, const int4 *__restrict__ tw, int post,
+            ColMasks64 mk)
 {
     using S = Fft64Shape<N>;
     extern __shared__ longlong2 sm64[];
     __shared__ unsigned s_hi[S::NTR];
     __shared__ int s_any;
+    // the column's tile mask (a CTA's NTR <= 16 columns share one tile column)
+    __shared__ unsigned char s_tm[N / 16];
     const int tid = threadIdx.x;
     const int t = tid / S::TPT, lt = tid - t * S::TPT;
     const int first = blockIdx.x * S::NTR;
     double2 *base = data + (size_t)blockIdx.y * (size_t)nx * (size_t)ny;
+    const bool masked = COLS && mk.on;
+    if (masked) {
+        const int tu = first >> mk.tsh;
+        if (!mk.col[(size_t)blockIdx.y * mk.ntu + tu]) return;   // a column nobody reads
+        for (int tv = tid; tv < mk.ntv; tv += S::THREADS)
+            s_tm[tv] = mk.tile[((size_t)blockIdx.y * mk.ntv + tv) * mk.ntu + tu];
+    }
 
     if (tid < S::NTR) s_hi[tid] = 0u;
     if (tid == 0) s_any = 0;
@@ -271,6 +290,7 @@ __global__ void __launch_bounds__(Fft64Shape<N>::THREADS, Fft64Shape<N>::MINB)
         fft64_elem<N, COLS>(f, first, nx, tt, i, g);
         const unsigned th = s_hi[tt];
         if (th == 0u) continue;   // zero transform: already zero in place
+        if (masked && !s_tm[i >> mk.tsh]) continue;   // a tile nobody reads
         double2 o;
         if ((th >> 20) == 2047u) {
             o.x = o.y = __longlong_as_double(0x7FF8000000000000ll);
@@ -307,7 +327,7 @@ __global__ void k_tw64(int4 *tw, int n)
 
 template <int N, int SIGN, bool COLS>
 cudaError_t launch_n(double2 *data, int nx, int ny, int planes, const int4 *tw, int post,
-                     cudaStream_t stream)
+                     cudaStream_t stream, const ColMasks64 &mk)
 {
     using S = Fft64Shape<N>;
     auto kern = k_fft64<N, SIGN, COLS>;
@@ -317,21 +337,21 @@ cudaError_t launch_n(double2 *data, int nx, int ny, int planes, const int4 *tw, 
     if (e != cudaSuccess) return e;
     const int count = COLS ? nx : ny;
     const dim3 grid(count / S::NTR, planes);
-    kern<<<grid, S::THREADS, S::SMEM, stream>>>(data, nx, ny, SIGN > 0 ? tw : tw + N, post);
+    kern<<<grid, S::THREADS, S::SMEM, stream>>>(data, nx, ny, SIGN > 0 ? tw : tw + N, post, mk);
     return cudaGetLastError();
 }
 
 template <int SIGN, bool COLS>
 cudaError_t launch_dir(double2 *data, int nx, int ny, int planes, const int4 *tw, int post,
-                       cudaStream_t stream)
+                       cudaStream_t stream, const ColMasks64 &mk = ColMasks64{})
 {
     switch (COLS ? ny : nx) {
-    case 256: return launch_n<256, SIGN, COLS>(data, nx, ny, planes, tw, post, stream);
-    case 512: return launch_n<512, SIGN, COLS>(data, nx, ny, planes, tw, post, stream);
-    case 1024: return launch_n<1024, SIGN, COLS>(data, nx, ny, planes, tw, post, stream);
-    case 2048: return launch_n<2048, SIGN, COLS>(data, nx, ny, planes, tw, post, stream);
-    case 4096: return launch_n<4096, SIGN, COLS>(data, nx, ny, planes, tw, post, stream);
-    case 8192: return launch_n<8192, SIGN, COLS>(data, nx, ny, planes, tw, post, stream);
+    case 256: return launch_n<256, SIGN, COLS>(data, nx, ny, planes, tw, post, stream, mk);
+    case 512: return launch_n<512, SIGN, COLS>(data, nx, ny, planes, tw, post, stream, mk);
+    case 1024: return launch_n<1024, SIGN, COLS>(data, nx, ny, planes, tw, post, stream, mk);
+    case 2048: return launch_n<2048, SIGN, COLS>(data, nx, ny, planes, tw, post, stream, mk);
+    case 4096: return launch_n<4096, SIGN, COLS>(data, nx, ny, planes, tw, post, stream, mk);
+    case 8192: return launch_n<8192, SIGN, COLS>(data, nx, ny, planes, tw, post, stream, mk);
     }
     return cudaErrorInvalidValue;
 }
@@ -351,12 +371,30 @@ cudaError_t build_twiddles64(int4 *tw, int n, cudaStream_t stream)
 }
 
 cudaError_t launch_fft64(double2 *data, int nx, int ny, int planes, int sign,
-                         const int4 *twx, const int4 *twy, int post, cudaStream_t stream)
+                         const int4 *twx, const int4 *twy, int post, cudaStream_t stream,
+                         const FftMasks *masks, int tsh)
 {
+    ColMasks64 mk{};
+    if (masks) {
+        mk.ntu = nx >> tsh;
+        mk.ntv = ny >> tsh;
+        mk.tsh = tsh;
+        // a CTA's columns must share one tile column
+        if ((1 << tsh) < 16 || mk.ntv > ny / 16) return cudaErrorInvalidValue;
+    }
     cudaError_t e;
     if (sign > 0) {
+        // (reading only the occupied tiles saved nothing here: the pass is
+        // bound by its integer arithmetic, and empty columns are skipped anyway)
         e = launch_dir<1, true>(data, nx, ny, planes, twy, 0, stream);
         if (e == cudaSuccess) e = launch_dir<1, false>(data, nx, ny, planes, twx, post, stream);
+    } else if (masks) {
+        // rows first, so that the column pass, last, writes only what is read
+        mk.tile = masks->need_tile;
+        mk.col = masks->need_col;
+        mk.on = true;
+        e = launch_dir<-1, false>(data, nx, ny, planes, twx, 0, stream);
+        if (e == cudaSuccess) e = launch_dir<-1, true>(data, nx, ny, planes, twy, post, stream, mk);
     } else {
         e = launch_dir<-1, true>(data, nx, ny, planes, twy, 0, stream);
         if (e == cudaSuccess) e = launch_dir<-1, false>(data, nx, ny, planes, twx, post, stream);

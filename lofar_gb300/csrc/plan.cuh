@@ -158,6 +158,7 @@ namespace wsg {
 
 WScreen plan_wscreen(const wsg_plan *p);
 FftMasks mask_view(const wsg_plan *p);
+int ensure_masks(wsg_plan *p);
 // Derived geometry, CTA counts and the fused-FFT switch from the plan's
 // sizes and tuning; drops the record capacity (bin tables depend on them).
 int plan_configure(wsg_plan *p);

@@ -265,8 +265,13 @@ bool fft_fused_supported(int nx, int ny, int tile);
 // entries per axis.  In place, unnormalised, times the exact power of two 2^post.
 bool fft64_supported(int nx, int ny, long long planes);
 cudaError_t build_twiddles64(int4 *tw, int n, cudaStream_t stream);
+// masks (optional, the plan's tile masks of its last binning; tile = 2^tsh;
+// used by the adjoint, sign -1): the row pass runs first, then the column
+// pass transforms only the tile columns the degridder reads and writes only
+// their needed tiles (the other cells of the output are left unspecified).
 cudaError_t launch_fft64(double2 *data, int nx, int ny, int planes, int sign,
-                         const int4 *twx, const int4 *twy, int post, cudaStream_t stream);
+                         const int4 *twx, const int4 *twy, int post, cudaStream_t stream,
+                         const FftMasks *masks = nullptr, int tsh = 0);
 cudaError_t launch_twiddles(float2 *tw, int n, cudaStream_t s);
 cudaError_t launch_fft_masks(const GeomParams &g, const BinBuffers &b, const FftMasks &m,
                              cudaStream_t s);
