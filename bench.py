@@ -80,7 +80,9 @@ def parse():
     ap.add_argument("--planes", type=int, default=None)
     ap.add_argument("--support", type=int, default=None)
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    # as many as the timed device steps: the first step's upload cannot
+    # overlap a previous step, a fill cost spread over the steps
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     a = ap.parse_args()
