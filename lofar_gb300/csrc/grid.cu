@@ -168,7 +168,6 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
     constexpr int RPT = kStageR / kThreadsR;     // staged records per thread
     constexpr int CPT = T * T / kThreadsR;
     constexpr int TP = T + 1;                    // accumulator pitch (odd)
-    constexpr int kNoCell = -(1 << 20);
     static_assert(KW >= 1 && NKEY / 2 == KW * kThreadsR, "bucket words per thread");
     static_assert(kStageR < 65536, "16-bit record indices and bucket counts");
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -402,6 +401,7 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
         }
         const float scale = ldexpf(1.0f, fexp);
         const float inv = ldexpf(1.0f, -fexp);
+        const float vscale = scale * norm;   // the row weight carries the kernel's norm
 
         const unsigned nst = one_stage ? 1u : (n + kStageR - 1) / kStageR;
         const unsigned per = nst ? (n + nst - 1) / nst : 0u;
@@ -441,23 +441,25 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
             int acc_r[NT], acc_i[NT];
 #pragma unroll
             for (int j = 0; j < NT; j++) acc_r[j] = acc_i[j] = 0;
-            int pcu = kNoCell, pcv = kNoCell;   // cell of the run being summed
+            // the run being summed: the cell bytes (bits 24..31) of its
+            // records' first two words; all ones before the first record, a
+            // cell outside every tile
+            unsigned px = 0xFFFFFFFFu, py = 0xFFFFFFFFu;
             for (unsigned t = 0; t < len; t++) {
                 const unsigned ri = sbeg + t;
                 const bool valid = lane_on && ri < cnt;
                 const uint4 q = stage[SORTED ? sidx[valid ? ri : 0u] : (valid ? ri : 0u)];
-                const int cu = (int)(q.x >> 24) - 64;
-                const int cv = (int)(q.y >> 24) - 64;
                 const float fu = (float)(q.x & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float fv = (float)(q.y & 0xFFFFFFu) * 1.1920928955078125e-7f - 1.0f;
                 const float du = off1 - fu, dv = off1 - fv;
-                const float gu = norm * fast_exp2(du * du * c2);
-                const float gv = fast_exp2(dv * dv * c2) * scale;
+                const float gu = fast_exp2(du * du * c2);
+                const float gv = fast_exp2(dv * dv * c2) * vscale;
                 const float ar = valid ? __uint_as_float(q.z) * gv : 0.0f;
                 const float ai = valid ? __uint_as_float(q.w) * gv : 0.0f;
-                const bool chg = valid && (cu != pcu || cv != pcv);
+                const bool chg = valid && ((q.x ^ px) | (q.y ^ py)) >= (1u << 24);
                 if (__any_sync(0xFFFFFFFFu, chg)) {
                     // the run ended: add its window row to the tile, restart
+                    const int pcu = (int)(px >> 24) - 64, pcv = (int)(py >> 24) - 64;
                     const int row = pcv - K + k;
                     const int col0 = pcu - K;
                     const bool rin = chg && row >= 0 && row < T;
@@ -472,8 +474,8 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
                     }
                 }
                 if (valid) {
-                    pcu = cu;
-                    pcv = cv;
+                    px = q.x;
+                    py = q.y;
                 }
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
@@ -485,6 +487,7 @@ __global__ void __launch_bounds__(f32c_threads(K), 2) k_grid_f32c(GridArgs a)
                 }
             }
             {
+                const int pcu = (int)(px >> 24) - 64, pcv = (int)(py >> 24) - 64;
                 const int row = pcv - K + k;
                 const int col0 = pcu - K;
                 if (lane_on && row >= 0 && row < T) {
