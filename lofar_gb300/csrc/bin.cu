@@ -500,6 +500,7 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
     static_assert(PREC == WSG_FP32C, "the walk serves FP32C plans");
     __shared__ double su[32][9], sv[32][9], sw[32][9];
     __shared__ float sr[32][9], si[32][9], st_[32][9];
+    __shared__ unsigned spos[32][9];   // each measurement's primary record, transposed back
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned nb = (unsigned)g.nbins;
     const bool single = nf == 1 && np == 1;
@@ -578,13 +579,46 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
                 r.rec16[p] = make_uint4(((unsigned)(cu + 64) << 24) | qu,
                                         ((unsigned)(cv + 64) << 24) | qv, __float_as_uint(re),
                                         __float_as_uint(im));
-                // only the degridder reads idx, and only of primaries
-                if (d == dp) r.idx[p] = (unsigned)m;
             }
         }
+        // the degridder writes its values in record order and the walk
+        // gathers them back: the map measurement -> primary record
+        unsigned pp = kFull;
+#pragma unroll
+        for (int d = 0; d < 4; d++) pp = (st == 0 && d == dp) ? pos[d] : pp;
+        spos[lane][warp] = pp;
         __syncthreads();   // the tile's inputs are read before the next tile's land
+        {
+            const long long mo = rows_m(wk, cur.tb, cur.bb, lt, lj);
+            if (mo >= 0) r.pos[mo] = spos[lt][lj];
+        }
         cur = nxt;
         walk_advance(wk, nxt, step);
+    }
+}
+
+// out[m] = vrec[pos[m]] along the walk: a tile's map entries are loaded by
+// dump segments, the values read by baseline (consecutive dumps of a track
+// sit in consecutive records) and written back by dump segments.
+__global__ void __launch_bounds__(256)
+k_walk_gather(RowsWalk wk, const unsigned *__restrict__ pos, const float2 *__restrict__ vrec,
+              float2 *__restrict__ out)
+{
+    __shared__ unsigned sp[32][9];
+    __shared__ float2 so[32][9];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lt = tid >> 3, lj = tid & 7;
+    const WalkPos step = walk_pos(wk, gridDim.x);
+    WalkPos cur = walk_pos(wk, blockIdx.x);
+    for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
+        const long long mo = rows_m(wk, cur.tb, cur.bb, lt, lj);
+        sp[lt][lj] = mo >= 0 ? __ldcs(pos + mo) : kFull;
+        __syncthreads();
+        const unsigned p = sp[lane][warp];
+        so[lane][warp] = p != kFull ? __ldcs(vrec + p) : make_float2(0.f, 0.f);
+        __syncthreads();
+        if (mo >= 0) out[mo] = so[lt][lj];
+        walk_advance(wk, cur, step);
     }
 }
 
@@ -954,6 +988,15 @@ int tile_grid(long long tiles)
 }  // namespace
 
 long long scan_blocks(long long nbins) { return (nbins + kScanPerBlock - 1) / kScanPerBlock; }
+
+cudaError_t launch_walk_gather(const GeomParams &g, long long n, const unsigned *pos,
+                               const float2 *vrec, float2 *out, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const RowsWalk w = make_rows_walk(n, g.rows);
+    k_walk_gather<<<tile_grid(w.tiles), 256, 0, s>>>(w, pos, vrec, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double *vv,
                              const double *ww, long long n, const BinBuffers &b, cudaStream_t s)

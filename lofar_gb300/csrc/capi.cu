@@ -345,7 +345,7 @@ int wsg_plan_destroy(wsg_plan *p)
         p->a_vis.release();
     }
     if (p->fft) cufftDestroy(p->fft);
-    DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rec16, &p->partials, &p->rcell, &p->rfrac, &p->rval, &p->ridx,
+    DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rec16, &p->partials, &p->rcell, &p->rfrac, &p->rval, &p->ridx, &p->rpos, &p->rvrec,
                       &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi, &p->h_wt, &p->h_image,
                       &p->h_out, &p->sinx, &p->siny, &p->wscreen, &p->fft_work};
     for (DevBuf *b : bufs) b->release();
@@ -451,7 +451,7 @@ long long wsg_plan_device_bytes(wsg_plan *p)
 {
     if (!p) return 0;
     const DevBuf *bufs[] = {&p->grid, &p->bins, &p->ctr, &p->rec16, &p->partials, &p->rcell, &p->rfrac, &p->rval,
-                            &p->ridx, &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi,
+                            &p->ridx, &p->rpos, &p->rvrec, &p->h_uu, &p->h_vv, &p->h_ww, &p->h_vr, &p->h_vi,
                             &p->h_wt, &p->h_image, &p->h_out, &p->sinx, &p->siny,
                             &p->wscreen, &p->fft_work};
     long long t = 0;
@@ -472,6 +472,10 @@ int wsg_bin(wsg_plan *p, long n, long nf, long np, const double *uu, const doubl
     if (n > 0 && (!uu || !vv || !ww || !vr || !vi || !wt))
         return set_error(WSG_ERR_ARG, "NULL input pointer");
     WSG_TRY(ensure_records(p, n));
+    if (rows_walk(p->geom, n)) {
+        WSG_CUDA(p->rpos.ensure(sizeof(unsigned) * (size_t)n));
+        WSG_CUDA(p->rvrec.ensure(sizeof(float2) * (size_t)p->rec_cap));
+    }
     const BinBuffers b = p->binbufs();
     WSG_CUDA(cudaMemsetAsync(b.sub_prim, 0, bin_counter_bytes(p->geom.nbins, b.nsub), p->stream));
     WSG_CUDA(cudaMemsetAsync(b.ctr, 0, sizeof(DevCounters), p->stream));
@@ -607,7 +611,7 @@ int wsg_degrid(wsg_plan *p, const void *grid, void *out)
     const BinBuffers b = p->binbufs();
     WSG_CUDA(cudaMemsetAsync(&b.ctr->work_degrid, 0, sizeof(unsigned), p->stream));
     WSG_CUDA(launch_degrid(p->geom, p->prec, b, p->recbufs(), grid, out, p->n_binned,
-                           p->ctas_degrid, p->stream));
+                           p->ctas_degrid, p->stream, p->walked));
     return WSG_OK;
 }
 

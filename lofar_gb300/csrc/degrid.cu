@@ -145,6 +145,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     const float off1 = (float)(kk - K) + 0.5f;
     const float2 *__restrict__ grid = reinterpret_cast<const float2 *>(a.grid);
     float2 *out = reinterpret_cast<float2 *>(a.out);
+    float2 *vrec = a.r.vrec;   // set: values in record order (the walk gathers them)
     const unsigned nsplit = a.b.ctr->nsplit_items;
     const unsigned nitems = nsplit + a.b.ctr->nwork;
     if (TMA && tid == 0) {
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
             __syncthreads();
             for (unsigned i = tid; i < cnt; i += kThreads) {
                 stage[i] = __ldcs(a.r.rec16 + off + c0 + i);
-                sidx[i] = __ldcs(a.r.idx + off + c0 + i);
+                if (!vrec) sidx[i] = __ldcs(a.r.idx + off + c0 + i);
             }
             __syncthreads();
             for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
@@ -232,7 +233,10 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
                     sr += __shfl_xor_sync(0xFFFFFFFFu, sr, d);
                     si += __shfl_xor_sync(0xFFFFFFFFu, si, d);
                 }
-                if (k == 0 && valid) out[sidx[r]] = make_float2(sr, si);
+                if (k == 0 && valid) {
+                    if (vrec) vrec[off + c0 + r] = make_float2(sr, si);   // record order
+                    else out[sidx[r]] = make_float2(sr, si);
+                }
             }
         }
     }
@@ -501,8 +505,10 @@ bool degrid_tma_timed_out()
 }
 
 cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b, const RecBuffers &r,
-                          const void *grid, void *out, long long n, int ctas, cudaStream_t s)
+                          const void *grid, void *out, long long n, int ctas, cudaStream_t s,
+                          bool walked)
 {
+    walked = walked && prec != WSG_FP64 && r.pos && r.vrec;
     CUtensorMap m;
     memset(&m, 0, sizeof(m));
     const bool tma = prec != WSG_FP64 && g.half <= kDegridTmaMaxHalf &&
@@ -511,17 +517,23 @@ cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b, co
     const void *k = degrid_pick(prec, g.tile, g.half, tma, smem);
     if (!k) return cudaErrorInvalidValue;
     const size_t esz = prec == WSG_FP64 ? sizeof(double2) : sizeof(float2);
-    cudaError_t e = cudaMemsetAsync(out, 0, (size_t)n * esz, s);
+    cudaError_t e = cudaSuccess;
+    // the walk's gather writes every output; otherwise measurements without
+    // a record (dropped) read zero
+    if (!walked) e = cudaMemsetAsync(out, 0, (size_t)n * esz, s);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     DegridArgs a{g, b, r, grid, out};
+    if (!walked) a.r.vrec = nullptr;
     if (prec == WSG_FP64) {
         void *args[] = {&a};
         return cudaLaunchKernel(k, dim3(ctas), dim3(kThreadsD64), args, smem, s);
     }
     void *args[] = {&a, &m};
-    return cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
+    e = cudaLaunchKernel(k, dim3(ctas), dim3(kThreads), args, smem, s);
+    if (e != cudaSuccess || !walked) return e;
+    return launch_walk_gather(g, n, r.pos, r.vrec, reinterpret_cast<float2 *>(out), s);
 }
 
 }  // namespace wsg

@@ -195,7 +195,7 @@ extern "C" int wsg_grid_noalloc(int num_w_planes, long num_points, long freq_per
     unsigned *bins = reinterpret_cast<unsigned *>(s + o_bins);
     bin_buffer_carve(bins, g.nbins, 1, b);
     b.split_size = kDefaultSplit;
-    RecBuffers r;
+    RecBuffers r{};
     r.rec16 = nullptr;
     r.cell = reinterpret_cast<unsigned *>(s + o_cell);
     r.idx = reinterpret_cast<unsigned *>(s + o_idx);

@@ -91,6 +91,7 @@ struct wsg_plan {
     wsg::DevBuf bins;                          // bin_buffer_bytes(nbins)
     wsg::DevBuf ctr;                           // DevCounters
     wsg::DevBuf rec16, rcell, rfrac, rval, ridx;   // records (FP32C: rec16+idx; FP64: SoA)
+    wsg::DevBuf rpos, rvrec;                       // the walk's record map and degridded values
     wsg::DevBuf partials;                      // FP32C partial tiles of split bins
     unsigned long long rec_cap = 0;
     long long n_binned = -1;                   // measurements (batch: visibilities) binned
@@ -150,6 +151,8 @@ struct wsg_plan {
         r.val = rval.p;
         r.idx = ridx.as<unsigned>();
         r.capacity = rec_cap;
+        r.pos = rpos.as<unsigned>();
+        r.vrec = rvrec.as<float2>();
         return r;
     }
 };

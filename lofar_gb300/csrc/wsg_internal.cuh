@@ -100,6 +100,11 @@ struct RecBuffers {
     void *val;    // double2
     unsigned *idx;
     unsigned long long capacity;
+    // the [dump][baseline] walk (FP32C): pos[m] = the record of measurement
+    // m's primary (0xFFFFFFFF: none); vrec[p] = the degridded value of
+    // primary record p, gathered to measurement order afterwards
+    unsigned *pos;
+    float2 *vrec;
 };
 
 // Bytes of BinBuffers storage for nbins bins with nsub sub-counters and at
@@ -180,6 +185,9 @@ cudaError_t launch_bin_count(const GeomParams &g, const double *uu, const double
                              const double *ww, long long n, const BinBuffers &b,
                              cudaStream_t s);
 cudaError_t launch_bin_scan(const GeomParams &g, const BinBuffers &b, cudaStream_t s);
+// out[m] = vrec[pos[m]] (zero where pos[m] is 0xFFFFFFFF) along the walk.
+cudaError_t launch_walk_gather(const GeomParams &g, long long n, const unsigned *pos,
+                               const float2 *vrec, float2 *out, cudaStream_t s);
 cudaError_t launch_bin_scatter(const GeomParams &g, int prec, const double *uu,
                                const double *vv, const double *ww, const float *vr,
                                const float *vi, const float *wt, long long n, long long nf,
@@ -222,9 +230,13 @@ cudaError_t launch_grid(const GeomParams &g, int prec, const BinBuffers &b,
 int grid_max_ctas_per_sm(int prec, int tile, int half);
 
 // ---- launchers (degrid.cu) ----
+// walked: the records came from the [dump][baseline] walk (FP32C); the
+// values are written in record order (r.vrec) and gathered to measurement
+// order along the walk (r.pos), every output written.  Otherwise each value
+// is stored at its measurement's index (r.idx) after a memset of `out`.
 cudaError_t launch_degrid(const GeomParams &g, int prec, const BinBuffers &b,
                           const RecBuffers &r, const void *grid, void *out, long long n,
-                          int ctas, cudaStream_t s);
+                          int ctas, cudaStream_t s, bool walked = false);
 int degrid_max_ctas_per_sm(int prec, int tile, int half);
 
 // ---- launchers (wcorrect.cu) ----
