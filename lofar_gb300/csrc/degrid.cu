@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
     constexpr int PW = tma_pitch<AW>();
     constexpr int AP0 = AW | 1;
     constexpr int NW = kThreads / 32;
+    constexpr int NS = NW * RPW;           // record streams per stage
     constexpr int AP = TMA ? PW : AP0;
     constexpr int TB = TMA ? (AW * PW * 8 + 127) / 128 * 128 : (AW * AP0 * 8 + 15) / 16 * 16;
     extern __shared__ __align__(TMA ? 128 : 16) unsigned char smraw[];
@@ -206,8 +207,15 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
                 if (!vrec) sidx[i] = __ldcs(a.r.idx + off + c0 + i);
             }
             __syncthreads();
-            for (unsigned base = warp * RPW; base < cnt; base += NW * RPW) {
-                const unsigned r = base + grp;
+            // each group takes a contiguous stream of the stage; lane k keeps
+            // row k of its record's window in registers and reloads it only
+            // when the cell changes (records of one track share cells)
+            const unsigned len = (cnt + NS - 1) / NS;
+            const unsigned sbeg = (unsigned)(warp * RPW + grp) * len;
+            float2 win[NT];
+            int wrow = -1;   // tile offset of the row held in win
+            for (unsigned t = 0; t < len; t++) {
+                const unsigned r = sbeg + t;
                 const bool valid = r < cnt;
                 const uint4 q = stage[valid ? r : 0];
                 const int cu = (int)(q.x >> 24) - 64;
@@ -218,13 +226,17 @@ __global__ void __launch_bounds__(kThreads) k_degrid_f32c(DegridArgs a, const __
                 const float gu = norm * fast_exp2(du * du * c2);
                 const float gv = on ? fast_exp2(dv * dv * c2) : 0.0f;
                 const int row = (cv - K + kk + H) * AP + (cu - K + H);
+                if (row != wrow) {
+#pragma unroll
+                    for (int j = 0; j < NT; j++) win[j] = tile[row + j];
+                    wrow = row;
+                }
                 float sr = 0.f, si = 0.f;
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
                     const float g = __shfl_sync(0xFFFFFFFFu, gu, grp * GS + j);
-                    const float2 t = tile[row + j];
-                    sr = fmaf(g, t.x, sr);
-                    si = fmaf(g, t.y, si);
+                    sr = fmaf(g, win[j].x, sr);
+                    si = fmaf(g, win[j].y, si);
                 }
                 sr *= gv;
                 si *= gv;
