@@ -599,26 +599,43 @@ k_bin_scatter_rows(GeomParams g, const double *__restrict__ uu, const double *__
 
 // out[m] = vrec[pos[m]] along the walk: a tile's map entries are loaded by
 // dump segments, the values read by baseline (consecutive dumps of a track
-// sit in consecutive records) and written back by dump segments.
+// sit in consecutive records) and written back by dump segments.  A CTA
+// takes kGatherTiles tiles at a time, so that every thread has as many
+// independent loads in flight.
+constexpr int kGatherTiles = 4;
+
 __global__ void __launch_bounds__(256)
 k_walk_gather(RowsWalk wk, const unsigned *__restrict__ pos, const float2 *__restrict__ vrec,
               float2 *__restrict__ out)
 {
-    __shared__ unsigned sp[32][9];
-    __shared__ float2 so[32][9];
+    constexpr int G = kGatherTiles;
+    __shared__ unsigned sp[G][32][9];
+    __shared__ float2 so[G][32][9];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int lt = tid >> 3, lj = tid & 7;
     const WalkPos step = walk_pos(wk, gridDim.x);
     WalkPos cur = walk_pos(wk, blockIdx.x);
-    for (long long q = blockIdx.x; q < wk.tiles; q += gridDim.x) {
-        const long long mo = rows_m(wk, cur.tb, cur.bb, lt, lj);
-        sp[lt][lj] = mo >= 0 ? __ldcs(pos + mo) : kFull;
+    for (long long q = blockIdx.x; q < wk.tiles; q += (long long)G * gridDim.x) {
+        long long mo[G];
+        WalkPos at = cur;
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            const bool in = q + (long long)k * gridDim.x < wk.tiles;
+            mo[k] = in ? rows_m(wk, at.tb, at.bb, lt, lj) : -1;
+            sp[k][lt][lj] = mo[k] >= 0 ? __ldcs(pos + mo[k]) : kFull;
+            walk_advance(wk, at, step);
+        }
         __syncthreads();
-        const unsigned p = sp[lane][warp];
-        so[lane][warp] = p != kFull ? __ldcs(vrec + p) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            const unsigned p = sp[k][lane][warp];
+            so[k][lane][warp] = p != kFull ? __ldcs(vrec + p) : make_float2(0.f, 0.f);
+        }
         __syncthreads();
-        if (mo >= 0) out[mo] = so[lt][lj];
-        walk_advance(wk, cur, step);
+#pragma unroll
+        for (int k = 0; k < G; k++)
+            if (mo[k] >= 0) out[mo[k]] = so[k][lt][lj];
+        cur = at;
     }
 }
 
