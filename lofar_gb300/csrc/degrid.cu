@@ -11,10 +11,15 @@
 // records of the bin are not visited: the halo makes every primary's window
 // local.
 //   FP32C: the tile + halo arrives by TMA (below; plain loads on odd-width
-//   grids), records are staged kStageD at a time; a group of 8 (or 16) lanes takes
-//   one record, lane k its row k: the row sum over the NT columns uses the
-//   column weights shuffled from the group's lanes, the row weight is applied
-//   once, and a shuffle tree over the group sums the rows.
+//   grids), records are staged kStageD at a time; a group of 8 (or 16) lanes
+//   takes a contiguous stream of the stage, one record at a time, lane k its
+//   row k: the row sum over the NT columns uses the column weights shuffled
+//   from the group's lanes and the window row, kept in registers while the
+//   records stay in one cell; the row weight is applied once, and a shuffle
+//   tree over the group sums the rows.  Records binned by the [dump][baseline]
+//   walk get their values stored in record order (vrec) and gathered back to
+//   measurement order by the walk (k_walk_gather); others are stored at
+//   their measurement's index.
 //   FP64: the same group-per-record layout, with the FP64 weights of
 //   taps64.cuh (several records per warp-wide exponential pass).
 #include <cuda.h>
