@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--layout", default="walk", choices=["walk", "index"],
+                    help="walk: the plan is told the measurements' [dump][baseline] layout "
+                         "(wsg_plan_set_layout) and bins along tracks; index: binning in "
+                         "index order, as for inputs of unknown layout")
     ap.add_argument("--shard", default="replicas", choices=["replicas", "planes"],
                     help="N>1: replicas (every GPU images the whole workload, no exchange) or "
                          "planes (one image; each GPU grids, transforms and w-corrects its "
@@ -357,7 +361,7 @@ def bench_ours(args, rank, world):
 
     # the synthetic measurements are [dump][baseline], as the reference's
     # measurement sets are (meta.txt's `baselines`): the binning walks tracks
-    rows = 0 if planes_mode else obs.meta.get("n_baselines", 0)
+    rows = 0 if planes_mode or args.layout == "index" else obs.meta.get("n_baselines", 0)
     plan = Plan(nx, ny, P, args.support, precision="fp32c")
     plan.set_wcorrection(res, obs.wmin, obs.wmax)
     plan.set_layout(rows)
@@ -392,7 +396,9 @@ def bench_ours(args, rank, world):
 
     result = dict(rank=rank, n=n, res=res, wmin=obs.wmin, wmax=obs.wmax, gen_s=gen_s,
                   ms_per_step=ms_per_step, value=value, per=per, stats=stats, clocks=clk,
-                  plan_bytes=plan.device_bytes(), l2=l2_note(flush))
+                  plan_bytes=plan.device_bytes(), l2=l2_note(flush),
+                  layout=(f"[dump][baseline] walk, {rows} rows per dump" if rows
+                          else "index order"))
 
     # -- plain FP64 form, same inputs --------------------------------------
     if not args.no_fp64 and rank == 0:
@@ -1150,7 +1156,8 @@ def main():
                    "precision": "FP32 complex grid, int32 fixed-point tile sums, FP64-exact "
                                 "coordinates and phase argument",
                    "parallelism": (f"planes{world}" if "planes" in res else f"replicas{world}"),
-                   "l2": res.get("l2", "inputs larger than L2 (no flush)")},
+                   "l2": res.get("l2", "inputs larger than L2 (no flush)"),
+                   "binning": res.get("layout", "index order")},
         "roofline": {"bound": "hbm", "kernel": "gridding stage (bin_count+bin_scan+bin_scatter+grid)",
                      "achieved": g["gbs"], "peak": peak, "unit": "GB/s", "frac": g["frac"],
                      "peak_source": f"{peak_kind} hbm copy bandwidth",
